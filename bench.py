@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""RVE homogenizations/s (stress + ctan) at 60^3 on one GB300.
+
+Workload (default): R = 32 damage RVEs of 60^3 elements (226,981 nodes, 680,943 DOF each): 4 stiff layers
+normal to z (E = 1e8, nu = 0.25, 0.1 thick), damage matrix (E = 1e7, nu = 0.25, Xt ~ U[1e5, 3e5] per RVE,
+seeded), FE_FULL coupling with lin_stress off, Newton <= 12 iterations at tolerance 1e-5, DPCG at the
+reference's 1e-5.  Each RVE has a seeded macro strain target ~ U[-2.5e-2, 2.5e-2]^6 (scaled up until the
+RVE is nonlinear).  Set-up loads every RVE to half its target and accepts the step; a bench step is one
+macro iteration: every RVE is homogenized (stress and ctan: one Newton solve plus six perturbed solves) at
+its target strain, through the public C ABI.  Inputs are synthetic (no dataset is involved).
+
+One JSON line is printed by rank 0.  `value` is the device-timed throughput (CUDA events on the handles'
+streams); `e2e` is the wall-clock throughput of the same C-ABI calls with host strain/stress/ctan buffers.
+`--impl reference` times the reference's CPU algorithm (the oracle port of it, since the compiled reference
+cannot run on this host) on all host cores, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RVE homogenizations/s (stress+ctan) at 60^3, adjoint+batched vs plain, 1 GB300"
+UNIT = "homogenizations/s"
+
+# Measured on a GB300 with this workload (n = 60, seeds below): CG iterations and Newton iterations of one
+# stress+ctan homogenization, averaged over the 32 RVEs.  The GPU arm prints its own figures every run; the
+# reference arm converts its bounded sample (one Newton iteration per RVE) into homogenizations/s with them.
+CG_ITS_PER_HOM = {60: None}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=60, help="elements per axis")
+    p.add_argument("--rves", type=int, default=32, help="RVEs per GPU")
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--cpu-sample-rves", type=int, default=0, help="RVEs in the CPU sample (default: host cores)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------------------
+# workload
+
+def workload(n, rves, seed, rank):
+    from micropp_gb300 import workloads as wl
+    xts = wl.damage_thresholds(rves, seed + 1000 * rank)
+    targets = wl.random_targets(rves, seed + 1000 * rank + 1, 2.5e-2)
+    return wl.layers_z(n), xts, targets
+
+
+def gpu_config(n, et, xt):
+    import micropp_gb300 as mg
+    mats = [mg.material(2, 1e7, 0.25, 0, 0, xt), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
+    return mg.config(n, mats=mats, coupling=[2], elem_type=et, lin_stress=0, nr_max_its=12, nr_max_tol=1e-5,
+                     calc_ctan_lin=0)
+
+
+# ---------------------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.rows, self.proc, self.gpu = [], None, gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------------------------------------
+# CPU sample: one Newton iteration per RVE on the oracle (the reference algorithm), OpenMP over RVEs
+
+def cpu_sample(n, xts, targets, cores):
+    """Times one Newton iteration (1 residual, 1 assembly, 1 DPCG solve, 1 residual) of `cores` RVEs of the
+    workload in parallel on the oracle, at the same preloaded state as the GPU arm's first Newton iteration
+    is not reproduced exactly: the sample starts from u = 0 at half the target strain.  Returns
+    (seconds, CG iterations summed over the sample RVEs)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as orc
+    from micropp_gb300 import workloads as wl
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    et = wl.layers_z(n)
+    # one handle per distinct Xt is needed for exact materials; the sample uses the first RVE's Xt for all
+    # `cores` points so the reference's own OpenMP loop over Gauss points (homogenize.cpp:72) runs them.
+    mats = [orc.material(2, 1e7, 0.25, 0, 0, float(xts[0])), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    cfg = orc.make_config(n, ngp=cores, mats=mats, coupling=[1] * cores, elem_type=et, lin_stress=0, nr_max_its=1,
+                          nr_max_tol=1e-5, calc_ctan_lin=0)
+    r = orc.OracleRVE(cfg)
+    for gp in range(cores):
+        r.set_strain(gp, 0.5 * targets[gp % len(targets)])
+    t0 = time.perf_counter()
+    r.homogenize()
+    dt = time.perf_counter() - t0
+    its = sum(r.newton(gp)[1] for gp in range(cores))
+    r.close()
+    return dt, its
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------------------------------------
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x, world):
+    if pg is None or world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return
+    cores = host_cores()
+    n = args.n
+    _, xts, targets = workload(n, args.rves, args.seed, 0)
+    per_hom = CG_ITS_PER_HOM.get(n)
+    if per_hom is None:
+        print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable":
+                          f"no measured CG-iterations-per-homogenization figure for n={n}"}))
+        return
+    samples = []
+    for _ in range(args.warmup + args.steps):
+        dt, its = cpu_sample(n, xts, targets, cores)
+        samples.append((dt, its))
+    timed = samples[args.warmup:]
+    tot_t = sum(s[0] for s in timed)
+    tot_its = sum(s[1] for s in timed)
+    value = tot_its / per_hom / tot_t
+    sample = (f"{args.steps} steps; each: one Newton iteration (residual, assembly, DPCG, residual) of {cores} "
+              f"RVEs of the workload in parallel (OpenMP over RVEs as the reference), "
+              f"{tot_its // max(args.steps, 1)} CG its per step; scaled by {per_hom:.0f} CG its per stress+ctan "
+              f"homogenization")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.rves} damage RVEs of {n}^3, 4 layers normal to z, stress+ctan",
+                   "n": n, "rves": args.rves},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def load_traffic(n):
+    """DRAM bytes per SpMV launch from the committed ncu summary (profiles/), if present."""
+    p = os.path.join(ROOT, "profiles", "spmv_fp64_traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("bytes_per_launch_at_n", {}).get(str(n))
+    return None
+
+
+def run_gpu(args):
+    world, rank, local, pg = dist_setup(args)
+    import ctypes
+
+    import micropp_gb300 as mg
+    from micropp_gb300 import build
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    build.build()
+    L = mg.load()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+    n, R = args.n, args.rves
+    et, xts, targets = workload(n, R, args.seed, rank)
+    handles = []
+    for i in range(R):
+        handles.append(mg.Micropp(gpu_config(n, et, float(xts[i]))))
+    # Set-up: load each RVE to half its target and accept the step; grow the target until it is nonlinear.
+    for i, h in enumerate(handles):
+        for _ in range(4):
+            h.set_strain(0, 0.5 * targets[i])
+            h.homogenize()
+            if h.is_non_linear(0):
+                break
+            targets[i] *= 1.5
+        h.update_vars()
+    nonlinear = sum(h.is_non_linear(0) for h in handles)
+
+    strain_bufs = [np.ascontiguousarray(t, dtype=np.float64) for t in targets]
+    out_s = np.zeros((R, 6))
+    out_c = np.zeros((R, 36))
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+
+    def step(k):
+        dev_ms = 0.0
+        for i, h in enumerate(handles):
+            e = strain_bufs[i] * (1.0 + 1e-3 * k)
+            L.micropp3_set_strain(ctypes.byref(h.h), 0, dp(e))
+            L.micropp3_homogenize(ctypes.byref(h.h))
+            L.micropp3_get_stress(ctypes.byref(h.h), 0, dp(out_s[i]))
+            L.micropp3_get_ctan(ctypes.byref(h.h), 0, dp(out_c[i]))
+            dev_ms += L.micropp3_last_homogenize_ms(ctypes.byref(h.h))
+        return dev_ms
+
+    for k in range(args.warmup):
+        step(k)
+    for h in handles:
+        h.set_kernel_timing(True)
+    cg0 = sum(h.total_cg_its() for h in handles)
+    l0 = sum(h.kernel_launches() for h in handles)
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for k in range(args.steps):
+            dev_ms += step(args.warmup + k)
+        wall = time.perf_counter() - t0
+    barrier(pg)
+    cg_its = sum(h.total_cg_its() for h in handles) - cg0
+    launches = sum(h.kernel_launches() for h in handles) - l0
+    if L.micropp3_last_error():
+        raise RuntimeError(L.micropp3_last_error().decode())
+    assert np.isfinite(out_s).all() and np.isfinite(out_c).all()
+    stats = {}
+    for fam in ("spmv", "cg_update", "assembly", "residual"):
+        tot = [h.kernel_stats(fam) for h in handles]
+        stats[fam] = (sum(t[0] for t in tot), sum(t[1] for t in tot), sum(t[2] for t in tot))
+    dev_s = max_over_ranks(pg, dev_ms / 1e3, world)
+    wall_s = max_over_ranks(pg, wall, world)
+    homs = R * args.steps * world
+    value = homs / dev_s
+    e2e = homs / wall_s
+    if rank != 0:
+        return
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peaks = json.load(open(pp))
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+    nk, ms, by = stats["spmv"]
+    achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
+    traffic = load_traffic(n)
+    nrow = 3 * (n + 1) ** 3
+    per_launch_bytes = nrow * (81 * 8 + 2 * 8)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cores = args.cpu_sample_rves or host_cores()
+        dt, its = cpu_sample(n, xts, targets, cores)
+        per_hom = cg_its / (R * args.steps)
+        cpu_val = its / per_hom / dt
+        cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": (f"one Newton iteration (residual, assembly, DPCG of {its // cores} its avg, residual) of "
+                          f"{cores} RVEs of the workload at half strain, OpenMP over RVEs, {dt:.1f} s; scaled by "
+                          f"{per_hom:.0f} CG its per stress+ctan homogenization measured in this run")}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{R} damage RVEs of {n}^3 per GPU (4 layers normal to z, Xt~U[1e5,3e5]), "
+                               f"FE_FULL stress+ctan (1 + 6 perturbed Newton solves), plain FP64 form",
+                   "n": n, "rves_per_gpu": R, "form": "plain-fp64", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (441 MB ELL per RVE)", "nonlinear_rves": nonlinear},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 6 * 8, "d2h_bytes_per_step": R * 42 * 8},
+        "roofline": {"bound": "hbm", "kernel": "k_cg_spmv (FP64 ELL SpMV + p.Ap)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "launches": nk, "avg_us": 1e3 * ms / nk if nk else None},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "cg_its_per_s": cg_its * world / dev_s,
+        "dof_updates_per_s": cg_its * nrow * world / dev_s,
+        "cg_its_per_homogenization": cg_its / (R * args.steps),
+        "kernels": {k: {"launches": v[0], "ms": v[1], "avg_us": 1e3 * v[1] / v[0] if v[0] else None,
+                        "algorithmic_GBps": v[2] / (v[1] / 1e3) / 1e9 if v[1] else None}
+                    for k, v in stats.items()},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,119 @@
+/*
+ * micropp_gb300.h -- extensions of the micropp3 C ABI served by the GB300 library.
+ *
+ * The reference's C wrapper fixes most micropp_params_t fields (micropp_c.cpp:33-58); these entry points
+ * expose the full parameter set of the C++ constructor (types.hpp:43-83), the GB300 solver options, per-RVE
+ * diagnostics and timing.  They add to the drop-in ABI of micropp_c.h and change none of it.
+ */
+#ifndef MICROPP_GB300_EXT_H
+#define MICROPP_GB300_EXT_H
+
+#include <stdbool.h>
+
+#include "micropp_c.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Coupling modes per macro point (types.hpp:110). */
+enum { MICROPP3_FE_LINEAR = 0, MICROPP3_FE_ONE_WAY = 1, MICROPP3_FE_FULL = 2, MICROPP3_MIX_RULE_CHAMIS = 3 };
+
+/* Arithmetic of the homogenization. */
+enum {
+  MICROPP3_FP64 = 0,  /* the reference algorithm in FP64 throughout (drop-in parity form) */
+  MICROPP3_MIXED = 1  /* FP32 Jacobian and CG inside FP64 iterative refinement; FP64 residual and averages */
+};
+
+/* How ctan is obtained for a nonlinear macro point. */
+enum {
+  MICROPP3_CTAN_PERTURB = 0,  /* the reference's 6 perturbed Newton solves (homogenize.cpp:256-275) */
+  MICROPP3_CTAN_IMPLICIT = 1  /* implicit differentiation at the converged state: one 6-RHS tangent solve */
+};
+
+/* Per-RVE status word of the last homogenize(). */
+enum {
+  MICROPP3_STATUS_OK = 0,
+  MICROPP3_STATUS_NEWTON_MAX_ITS = 1, /* Newton stopped at nr_max_its without meeting its tolerance */
+  MICROPP3_STATUS_CG_MAX_ITS = 2,     /* a linear solve stopped at cg_max_its */
+  MICROPP3_STATUS_NONFINITE = 4       /* a residual norm or an average stress was NaN or Inf */
+};
+
+/* Full construction parameters: the fields of micropp_params_t (types.hpp:43-63) in C form, plus the
+ * GB300 options.  Fill with micropp3_config_default() and override. */
+struct micropp3_config {
+  int ngp;
+  int size[3];            /* nodes per axis (elements + 1) */
+  int micro_type;         /* MIC_* (types.hpp:85-99) */
+  double geo_params[4];
+  struct material_base materials[3];
+  const int *coupling;    /* ngp entries; NULL = FE_ONE_WAY everywhere (micropp.cpp:88-96) */
+  int subiterations;
+  int nsubiterations;
+  int mpi_rank;
+  int nr_max_its;
+  double nr_max_tol;
+  double nr_rel_tol;
+  int cg_max_its;         /* honoured (the reference ignores it and uses CG_MAX_ITS = 1000) */
+  double cg_abs_tol;      /* honoured (reference: CG_ABS_TOL = 1e-50) */
+  double cg_rel_tol;      /* honoured (reference: CG_REL_TOL = 1e-5) */
+  int calc_ctan_lin;
+  int use_A0;             /* accepted for layout compatibility; the GPU path always assembles K */
+  int its_with_A0;
+  int lin_stress;
+  int write_log;
+  const int *elem_type;   /* optional element phase map, nelem entries in glo_elem order (0, 1 or 2) */
+  int precision;          /* MICROPP3_FP64 | MICROPP3_MIXED */
+  int ctan_mode;          /* MICROPP3_CTAN_PERTURB | MICROPP3_CTAN_IMPLICIT */
+  int reserved[4];        /* zero */
+};
+
+/* The reference defaults (types.hpp:43-63 with params.hpp:32-35 and ell.hpp:33-35), FP64, perturbation
+ * ctan. */
+void micropp3_config_default(struct micropp3_config *cfg);
+
+/* Construct from the full parameter set.  On failure self->ptr is NULL and micropp3_last_error() says why. */
+void micropp3_new_ext(struct micropp3 *self, const struct micropp3_config *cfg);
+
+/* Message of the last failure in this thread ("" if none), and its reset. */
+const char *micropp3_last_error(void);
+void micropp3_clear_error(void);
+
+/* Homogenize several handles in one batched pass (RVEs of different sizes and materials). */
+void micropp3_homogenize_many(struct micropp3 *const *handles, int n);
+
+/* Status word (MICROPP3_STATUS_*) of macro point gp after the last homogenize(). */
+int micropp3_get_status(const struct micropp3 *self, int gp_id);
+
+/* Newton iterations and CG iterations of the last main solve of gp. */
+void micropp3_get_newton(const struct micropp3 *self, int gp_id, int *its, int *solver_its, int *converged);
+
+/* Sizes: number of elements and of displacement unknowns of one RVE. */
+int micropp3_get_nelem(const struct micropp3 *self);
+int micropp3_get_nndim(const struct micropp3 *self);
+
+/* Copies of device state.  which = 0 selects vars_n / u_n, 1 selects vars_k / u_k.  Internal variables are
+ * 7 doubles per Gauss point in the reference order (params.hpp:41); zeros while the point is linear. */
+void micropp3_get_vars(const struct micropp3 *self, int gp_id, int which, double *out);
+void micropp3_get_u(const struct micropp3 *self, int gp_id, int which, double *out);
+void micropp3_get_elem_type(const struct micropp3 *self, int *out);
+void micropp3_get_ctan_lin(const struct micropp3 *self, double *out36);
+
+/* Device time of the last homogenize() (CUDA events on the handle's stream), in milliseconds. */
+double micropp3_last_homogenize_ms(const struct micropp3 *self);
+
+/* Kernel timing.  When enabled, every launch of the named kernel family is bracketed by CUDA events on the
+ * launching stream; micropp3_kernel_stats returns the launch count, the summed device time (ms) and the
+ * algorithmic bytes moved by those launches.  Families: "spmv", "cg_update", "assembly", "residual". */
+void micropp3_set_kernel_timing(struct micropp3 *self, int enable);
+int micropp3_kernel_stats(const struct micropp3 *self, const char *family, long *launches, double *ms,
+                          double *bytes);
+
+/* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
+long micropp3_total_cg_its(const struct micropp3 *self);
+long micropp3_kernel_launches(const struct micropp3 *self);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,82 @@
+// device.cuh -- data layout shared by the host engine and the sm_103a kernels.
+//
+// One RVE is a structured grid of nx*ny*nz nodes on the unit cube with 3 displacement unknowns per node
+// (row = node*3 + d, node = (k*ny + j)*nx + i, as in the reference, ell.hpp:37-39) and nex*ney*nez hex8
+// elements with 8 Gauss points each (element e = (ez*ney + ey)*nex + ex, params.hpp:37).
+//
+// HBM layout per RVE instance ("slot" of the batch):
+//   vectors u, du, b, r, z, p, Ap, kinv      nndim doubles each, node-interleaved (the reference layout)
+//   ELL values                               243 * np values: entry (s, fi, fj) of node n at
+//                                            [(s*9 + fi*3 + fj) * np + n], s = stencil slot 0..26 ordered
+//                                            (dz,dy,dx) in {-1,0,1}^3 (ell-common.cpp:95-134).  Columns are
+//                                            implicit; boundary rows are identity rows and are not stored.
+//   element residual blocks be               24 * nelem doubles, [(a*3+d) * nelem + e]
+//   internal variables                       7 doubles per Gauss point, [(e*8 + g)*7 + v] (params.hpp:41)
+#pragma once
+
+#include <stdint.h>
+
+namespace mgb {
+
+constexpr int kNvoi = 6;
+constexpr int kNpe = 8;
+constexpr int kNvarGp = 7;
+constexpr int kEllPerNode = 243;  // 27 stencil nodes x 3 x 3
+
+struct MeshDev {
+  int nx, ny, nz, nxny, nn, np;  // np: padded node stride of the ELL arrays
+  int nex, ney, nez, nelem;
+  double lx, ly, lz, dx, dy, dz, wg, vol_tot;
+};
+
+// A material with the constants its laws need precomputed on the host by the same expressions the
+// reference evaluates at every call (material.cpp:205-225, 110-147), so the values are identical.
+struct MatDev {
+  double E, nu, Ka, Sy, k, mu, lambda, Xt;
+  double two_mu;       // 2 * mu
+  double xt_thr;       // Xt / sqrt(E)
+  double dmg_r0, dmg_q0, dmg_q1, dmg_r1;
+  double pl_den;       // 2. * mu * (1. + Ka / (3. * mu))
+  int type;            // 0 elastic, 1 plastic (J2), 2 damage
+  int pad;
+};
+
+struct Mats {
+  MatDev m[3];
+};
+
+// Per-instance CG scalars, read and written only on the device.
+struct CgState {
+  double rz, pnorm0, pnorm, alpha, beta, pAp;
+  double min_err, rel_err;
+  int its, max_its, done, pad;
+};
+
+// Small per-instance outputs read back by the host.
+struct InstOut {
+  double norm;         // ||b||_2 of the last residual evaluation
+  double sig[6];       // volume-averaged stress of the last residual evaluation
+  int cg_its;          // iterations of the last CG solve
+  int nonlinear;       // OR of the evolute flags of the last update pass
+  int nonfinite;       // a reduction produced NaN/Inf
+  int cg_maxed;        // the last CG solve stopped at max_its
+};
+
+struct Inst {
+  double *u, *du, *b, *r, *z, *p, *Ap, *kinv, *vals, *be;
+  const double *vars_old;  // NULL: every law reads zeros (the reference's nullptr history)
+  double *vars_new;
+  double *red;             // reduction partials, kRedStride doubles per block
+  unsigned int *ticket;    // last-block counter for the reductions
+  CgState *cg;
+  InstOut *out;
+  double strain[6];
+  int has_vars_old;        // J2 evolute writes only when a history buffer exists (material.cpp:168-181)
+  int pad;
+};
+
+constexpr int kRedStride = 8;
+constexpr int kNodeBlock = 256;
+constexpr int kElemBlock = 128;
+
+}  // namespace mgb

@@ -1,0 +1,952 @@
+// engine.cpp -- host orchestration of the GB300 homogenization (see engine.hpp).
+//
+// This file is compiled with -ffp-contract=off: the few FP64 quantities formed on the host (shape
+// function gradients, the elastic phase stiffness, material constants, the mixture-rule tangent) are then
+// rounded exactly as the reference rounds them.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+
+#include "launch.h"
+#include "microstructure.hpp"
+
+namespace mgb {
+
+namespace {
+
+constexpr double kConstXg = 0.577350269189626;  // params.hpp:34
+constexpr double kDepsCtanAve = 1.0e-8;        // params.hpp:32
+
+const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+void check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+  }
+}
+
+void check_launch(int e, const char *what) { check((cudaError_t)e, what); }
+
+template <typename T>
+T *dalloc(size_t n, const char *what) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  check(cudaMalloc(&p, n * sizeof(T)), what);
+  return (T *)p;
+}
+
+void dfree(void *p) {
+  if (p) cudaFree(p);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Construction (micropp.cpp:29-171)
+
+Engine::Engine(const micropp3_config &cfg) {
+  if (cfg.ngp <= 0) throw std::invalid_argument("ngp must be positive");
+  for (int d = 0; d < 3; ++d)
+    if (cfg.size[d] < 2) throw std::invalid_argument("size[] must be at least 2 nodes per axis");
+  ngp_ = cfg.ngp;
+  micro_type_ = cfg.micro_type;
+  mpi_rank_ = cfg.mpi_rank;
+  std::memcpy(geo_params_, cfg.geo_params, sizeof(geo_params_));
+  for (int i = 0; i < 3; ++i) mat_in_[i] = cfg.materials[i];
+  nr_max_its_ = cfg.nr_max_its;
+  nr_max_tol_ = cfg.nr_max_tol;
+  nr_rel_tol_ = cfg.nr_rel_tol;
+  cg_max_its_ = cfg.cg_max_its;
+  cg_abs_tol_ = cfg.cg_abs_tol;
+  cg_rel_tol_ = cfg.cg_rel_tol;
+  lin_stress_ = cfg.lin_stress != 0;
+  subiterations_ = cfg.subiterations != 0;
+  nsubiterations_ = cfg.nsubiterations;
+  calc_ctan_lin_ = cfg.calc_ctan_lin != 0;
+  precision_ = cfg.precision;
+  ctan_mode_ = cfg.ctan_mode;
+  if (precision_ != MICROPP3_FP64) throw std::invalid_argument("this build serves precision = MICROPP3_FP64 only");
+  if (ctan_mode_ != MICROPP3_CTAN_PERTURB)
+    throw std::invalid_argument("this build serves ctan_mode = MICROPP3_CTAN_PERTURB only");
+
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    throw std::runtime_error("no CUDA device is available: the GB300 homogenization library has no CPU path");
+
+  build_mesh(cfg);
+  build_elem_types(cfg);
+  build_materials(cfg);
+  build_phase_stiffness();
+
+  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  check(cudaEventCreate(&ev0_), "event");
+  check(cudaEventCreate(&ev1_), "event");
+  d_etype_ = dalloc<int8_t>(mesh_.nelem, "elem_type");
+  check(cudaMemcpy(d_etype_, etype_.data(), mesh_.nelem, cudaMemcpyHostToDevice), "elem_type upload");
+  d_dsh_ = dalloc<double>(192, "dsh");
+  check(cudaMemcpy(d_dsh_, dsh_, sizeof(dsh_), cudaMemcpyHostToDevice), "dsh upload");
+  d_ke_ = dalloc<double>(3 * 576, "ke");
+  check(cudaMemcpy(d_ke_, ke_phase_, sizeof(ke_phase_), cudaMemcpyHostToDevice), "ke upload");
+  check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
+  d_count_ = dalloc<unsigned int>(1, "count");
+
+  gps_.resize(ngp_);
+  int n_fe = 0;
+  for (int i = 0; i < ngp_; ++i) {
+    GpState &g = gps_[i];
+    g.coupling = cfg.coupling ? cfg.coupling[i] : MICROPP3_FE_ONE_WAY;
+    if (g.coupling < MICROPP3_FE_LINEAR || g.coupling > MICROPP3_MIX_RULE_CHAMIS)
+      throw std::invalid_argument("coupling must be FE_LINEAR, FE_ONE_WAY, FE_FULL or MIX_RULE_CHAMIS");
+    if (!cfg.coupling || g.coupling == MICROPP3_FE_ONE_WAY || g.coupling == MICROPP3_FE_FULL) {
+      g.u_n = dalloc<double>(nndim(), "u_n");
+      g.u_k = dalloc<double>(nndim(), "u_k");
+      check(cudaMemsetAsync(g.u_n, 0, nndim() * sizeof(double), stream_), "u_n zero");
+      check(cudaMemsetAsync(g.u_k, 0, nndim() * sizeof(double), stream_), "u_k zero");
+    }
+    if (g.coupling != MICROPP3_MIX_RULE_CHAMIS) n_fe++;
+  }
+
+  // calc_volume_fractions (micropp.cpp:609-627)
+  const double evol = mesh_.dx * mesh_.dy * mesh_.dz;
+  Vm_ = Vf_ = 0.0;
+  for (int e = 0; e < mesh_.nelem; ++e) {
+    if (etype_[e] == 0)
+      Vm_ += evol;
+    else if (etype_[e] >= 1)
+      Vf_ += evol;
+  }
+  Vm_ /= mesh_.vol_tot;
+  Vf_ /= mesh_.vol_tot;
+
+  std::memset(ctan_lin_, 0, sizeof(ctan_lin_));
+  if (calc_ctan_lin_ && n_fe > 0) calc_ctan_lin();
+  for (auto &g : gps_) {
+    if (g.coupling == MICROPP3_MIX_RULE_CHAMIS)
+      ctan_mix_rule_chamis(g.ctan);
+    else
+      std::memcpy(g.ctan, ctan_lin_, sizeof(ctan_lin_));
+  }
+  sync();
+}
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto &g : gps_) {
+    dfree(g.u_n);
+    dfree(g.u_k);
+    dfree(g.vars_n);
+    dfree(g.vars_k);
+  }
+  free_slots();
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_})
+    for (auto &e : t->pool) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+  dfree(d_etype_);
+  dfree(d_dsh_);
+  dfree(d_ke_);
+  dfree(d_count_);
+  if (h_count_) cudaFreeHost(h_count_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::build_mesh(const micropp3_config &cfg) {
+  MeshDev &m = mesh_;
+  m.nx = cfg.size[0];
+  m.ny = cfg.size[1];
+  m.nz = cfg.size[2];
+  m.nxny = m.nx * m.ny;
+  const long long nn = (long long)m.nx * m.ny * m.nz;
+  if (nn * kEllPerNode > 2000000000LL)
+    throw std::invalid_argument("RVE too large for one device instance (at most ~8.2M nodes)");
+  m.nn = (int)nn;
+  m.np = (m.nn + 31) & ~31;
+  m.nex = m.nx - 1;
+  m.ney = m.ny - 1;
+  m.nez = m.nz - 1;
+  m.nelem = m.nex * m.ney * m.nez;
+  m.lx = m.ly = m.lz = 1.0;
+  m.dx = m.lx / m.nex;
+  m.dy = m.ly / m.ney;
+  m.dz = m.lz / m.nez;
+  m.wg = m.dx * m.dy * m.dz / kNpe;
+  m.vol_tot = m.lx * m.ly * m.lz;
+  // calc_bmat (micro3D.cpp:80-120): gradient of shape function i at Gauss point gp, formed as
+  // (s_a (1 + s_b xi_b)) (1 + s_c xi_c) / 8 * 2 / h, the reference's expression with the signs factored.
+  const double h[3] = {m.dx, m.dy, m.dz};
+  for (int gp = 0; gp < 8; ++gp) {
+    double xg[3];
+    for (int d = 0; d < 3; ++d) xg[d] = kCorner[gp][d] ? kConstXg : -kConstXg;
+    for (int i = 0; i < 8; ++i) {
+      double s[3], g[3];
+      for (int d = 0; d < 3; ++d) s[d] = kCorner[i][d] ? 1.0 : -1.0;
+      for (int d = 0; d < 3; ++d) {
+        const int p = (d == 0) ? 1 : 0, q = (d == 2) ? 1 : 2;
+        const double f1 = 1 + s[p] * xg[p];
+        const double f2 = 1 + s[q] * xg[q];
+        g[d] = s[d] * f1 * f2 / 8. * 2. / h[d];
+        dsh_[gp * 24 + i * 3 + d] = g[d];
+      }
+      double *B = &bmat_[gp][0][0];
+      const int c = i * 3;
+      for (int r = 0; r < 6; ++r) B[r * 24 + c] = B[r * 24 + c + 1] = B[r * 24 + c + 2] = 0.0;
+      B[0 * 24 + c] = g[0];
+      B[1 * 24 + c + 1] = g[1];
+      B[2 * 24 + c + 2] = g[2];
+      B[3 * 24 + c] = g[1];
+      B[3 * 24 + c + 1] = g[0];
+      B[4 * 24 + c] = g[2];
+      B[4 * 24 + c + 2] = g[0];
+      B[5 * 24 + c + 1] = g[2];
+      B[5 * 24 + c + 2] = g[1];
+    }
+  }
+}
+
+void Engine::build_elem_types(const micropp3_config &cfg) {
+  const MeshDev &m = mesh_;
+  etype_.resize(m.nelem);
+  for (int ez = 0; ez < m.nez; ++ez)
+    for (int ey = 0; ey < m.ney; ++ey)
+      for (int ex = 0; ex < m.nex; ++ex) {
+        const int e = (ez * m.ney + ey) * m.nex + ex;
+        const int t = cfg.elem_type ? cfg.elem_type[e]
+                                    : micro_elem_type(micro_type_, geo_params_, ex, ey, ez, m.dx, m.dy, m.dz);
+        if (t < 0 || t > 2) {
+          std::ostringstream os;
+          os << "element " << e << " has phase " << t << " (micro_type " << micro_type_
+             << "); phases must be 0, 1 or 2";
+          throw std::invalid_argument(os.str());
+        }
+        etype_[e] = (int8_t)t;
+      }
+}
+
+// Material constants with the expressions of material.hpp:73-135 and material.cpp:205-225.
+void Engine::build_materials(const micropp3_config &cfg) {
+  for (int i = 0; i < 3; ++i) {
+    const material_base &b = cfg.materials[i];
+    MatDev &d = mats_.m[i];
+    if (b.type < 0 || b.type > 2) throw std::invalid_argument("material type must be 0, 1 or 2");
+    d.type = b.type;
+    d.E = b.E;
+    d.nu = b.nu;
+    d.k = b.E / (3. * (1. - 2. * b.nu));
+    d.mu = b.E / (2. * (1. + b.nu));
+    d.lambda = b.nu * b.E / ((1. + b.nu) * (1. - 2. * b.nu));
+    d.Ka = (b.type == 1) ? b.Ka : -1.0;
+    d.Sy = (b.type == 1) ? b.Sy : -1.0;
+    d.Xt = (b.type == 2) ? b.Xt : -1.0;
+    d.two_mu = 2 * d.mu;
+    const double sqE = std::sqrt(d.E);
+    d.xt_thr = d.Xt / sqE;
+    const double Ey = 10.0e4, inf_Ey = 10. * Ey, H0 = 10.0;
+    d.dmg_r0 = Ey / sqE;
+    d.dmg_q0 = d.dmg_r0;
+    d.dmg_q1 = inf_Ey / sqE;
+    d.dmg_r1 = d.dmg_r0 + (d.dmg_q1 - d.dmg_q0) / H0;
+    d.pl_den = 2. * d.mu * (1. + d.Ka / (3. * d.mu));
+  }
+}
+
+// Element stiffness of an elastic phase, get_elem_mat (assembly.cpp:140-178) with the elastic ctan
+// (material.cpp:84-95).  B and wg are uniform over the mesh, so one Ke serves every element of the phase.
+void Engine::build_phase_stiffness() {
+  for (int ph = 0; ph < 3; ++ph) {
+    const MatDev &m = mats_.m[ph];
+    double C[36] = {0};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) C[i * 6 + j] += m.lambda;
+    for (int i = 0; i < 3; ++i) C[i * 6 + i] += 2 * m.mu;
+    for (int i = 3; i < 6; ++i) C[i * 6 + i] = m.mu;
+    double *K = ke_phase_[ph];
+    std::memset(K, 0, 576 * sizeof(double));
+    for (int gp = 0; gp < 8; ++gp) {
+      double cxb[6][24];
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 24; ++j) {
+          double t = 0.0;
+          for (int k = 0; k < 6; ++k) t += C[i * 6 + k] * bmat_[gp][k][j];
+          cxb[i][j] = t * mesh_.wg;
+        }
+      for (int mm = 0; mm < 6; ++mm)
+        for (int i = 0; i < 24; ++i) {
+          const double bmi = bmat_[gp][mm][i];
+          for (int j = 0; j < 24; ++j) K[i * 24 + j] += bmi * cxb[mm][j];
+        }
+    }
+  }
+}
+
+// calc_ctan_lin_mix_rule_Chamis (micropp.cpp:286-331).
+void Engine::ctan_mix_rule_chamis(double *ctan) const {
+  const double Em = mat_in_[0].E, nu_m = mat_in_[0].nu, Gm = Em / (2 * (1 + nu_m));
+  const double Ef = mat_in_[1].E, nu_f = mat_in_[1].nu, Gf = Ef / (2 * (1 + nu_f));
+  const double E11 = Vf_ * Ef + Vm_ * Em;
+  const double E22 = Em / (1 - std::sqrt(Vf_) * (1 - Em / Ef));
+  const double nu12 = Vf_ * nu_f + Vm_ * nu_m;
+  const double G12 = Gm / (1 - std::sqrt(Vf_) * (1 - Gm / Gf));
+  const double nu23 = nu12;
+  const double S[3][3] = {{1 / E11, -nu12 / E11, -nu12 / E11},
+                          {-nu12 / E11, 1 / E22, -nu23 / E22},
+                          {-nu12 / E11, -nu23 / E22, 1 / E22}};
+  const double det = S[0][0] * (S[1][1] * S[2][2] - S[2][1] * S[1][2]) -
+                     S[0][1] * (S[1][0] * S[2][2] - S[2][0] * S[1][2]) +
+                     S[0][2] * (S[1][0] * S[2][1] - S[2][0] * S[1][1]);
+  double Si[3][3];
+  Si[0][0] = +(S[1][1] * S[2][2] - S[2][1] * S[1][2]) / det;
+  Si[0][1] = -(S[1][0] * S[2][2] - S[2][0] * S[1][2]) / det;
+  Si[0][2] = +(S[1][0] * S[2][1] - S[2][0] * S[1][1]) / det;
+  Si[1][0] = -(S[0][1] * S[2][2] - S[2][1] * S[0][2]) / det;
+  Si[1][1] = +(S[0][0] * S[2][2] - S[2][0] * S[0][2]) / det;
+  Si[1][2] = -(S[0][0] * S[2][1] - S[2][0] * S[0][1]) / det;
+  Si[2][0] = +(S[0][1] * S[1][2] - S[1][1] * S[0][2]) / det;
+  Si[2][1] = -(S[0][0] * S[1][2] - S[1][0] * S[0][2]) / det;
+  Si[2][2] = +(S[0][0] * S[1][1] - S[1][0] * S[0][1]) / det;
+  std::memset(ctan, 0, 36 * sizeof(double));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) ctan[i * 6 + j] = Si[i][j];
+  ctan[3 * 6 + 3] = G12;
+  ctan[4 * 6 + 4] = G12;
+  ctan[5 * 6 + 5] = G12;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Workspace slots
+
+void Engine::ensure_slots(int n) {
+  if ((int)slots_.size() >= n) return;
+  const int old = (int)slots_.size();
+  const size_t nd = nndim(), nv = nvars();
+  const int nblocks = std::max((mesh_.nn + kNodeBlock - 1) / kNodeBlock, (mesh_.nelem + kElemBlock - 1) / kElemBlock) + 8;
+  slots_.resize(n);
+  for (int s = old; s < n; ++s) {
+    Slot &w = slots_[s];
+    w.u = dalloc<double>(nd, "u");
+    w.du = dalloc<double>(nd, "du");
+    w.b = dalloc<double>(nd, "b");
+    w.r = dalloc<double>(nd, "r");
+    w.z = dalloc<double>(nd, "z");
+    w.p = dalloc<double>(nd, "p");
+    w.Ap = dalloc<double>(nd, "Ap");
+    w.kinv = dalloc<double>(nd, "kinv");
+    w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
+    w.be = dalloc<double>((size_t)24 * mesh_.nelem, "element residuals");
+    w.vars_aux = dalloc<double>(nv, "vars_new_aux");
+    w.red = dalloc<double>((size_t)nblocks * kRedStride, "partials");
+    w.ticket = dalloc<unsigned int>(1, "ticket");
+    w.cg = dalloc<CgState>(1, "cg state");
+    w.out = dalloc<InstOut>(1, "out");
+    check(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), stream_), "ticket");
+    check(cudaMemsetAsync(w.out, 0, sizeof(InstOut), stream_), "out");
+    check(cudaMemsetAsync(w.p, 0, nd * sizeof(double), stream_), "p");
+  }
+  dfree(d_insts_);
+  d_insts_ = dalloc<Inst>(n, "insts");
+  if (h_out_) cudaFreeHost(h_out_);
+  check(cudaMallocHost((void **)&h_out_, n * sizeof(InstOut)), "pinned out");
+  h_insts_.assign(n, Inst{});
+  for (int s = 0; s < n; ++s) {
+    const Slot &w = slots_[s];
+    Inst &I = h_insts_[s];
+    I.u = w.u; I.du = w.du; I.b = w.b; I.r = w.r; I.z = w.z; I.p = w.p; I.Ap = w.Ap; I.kinv = w.kinv;
+    I.vals = w.vals; I.be = w.be; I.red = w.red; I.ticket = w.ticket; I.cg = w.cg; I.out = w.out;
+    I.vars_old = nullptr;
+    I.vars_new = w.vars_aux;
+  }
+  if (list_cap_ < n) {
+    dfree(d_list_);
+    d_list_ = dalloc<int>(n, "list");
+    list_cap_ = n;
+  }
+}
+
+void Engine::free_slots() {
+  for (auto &w : slots_) {
+    for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red}) dfree(p);
+    dfree(w.ticket);
+    dfree(w.cg);
+    dfree(w.out);
+  }
+  slots_.clear();
+  dfree(d_insts_);
+  d_insts_ = nullptr;
+  dfree(d_list_);
+  d_list_ = nullptr;
+  list_cap_ = 0;
+  if (h_out_) cudaFreeHost(h_out_);
+  h_out_ = nullptr;
+}
+
+void Engine::upload_insts() {
+  check(cudaMemcpyAsync(d_insts_, h_insts_.data(), h_insts_.size() * sizeof(Inst), cudaMemcpyHostToDevice, stream_),
+        "insts upload");
+}
+
+void Engine::upload_list(const std::vector<int> &slots) {
+  check(cudaMemcpyAsync(d_list_, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, stream_),
+        "list upload");
+  // The host vector may change right after; wait for the copy of pageable memory to be consumed.
+  check(cudaStreamSynchronize(stream_), "list sync");
+}
+
+void Engine::download_out() {
+  for (size_t s = 0; s < slots_.size(); ++s)
+    check(cudaMemcpyAsync(&h_out_[s], slots_[s].out, sizeof(InstOut), cudaMemcpyDeviceToHost, stream_), "out");
+  sync();
+}
+
+void Engine::sync() { check(cudaStreamSynchronize(stream_), "stream synchronize"); }
+
+void Engine::timer_begin(KernelTimer &t, double bytes) {
+  if (!t.enabled) return;
+  if (t.used == t.pool.size()) {
+    cudaEvent_t a, b;
+    check(cudaEventCreate(&a), "timer event");
+    check(cudaEventCreate(&b), "timer event");
+    t.pool.emplace_back(a, b);
+  }
+  check(cudaEventRecord(t.pool[t.used].first, stream_), "timer record");
+  t.pending_bytes += bytes;
+}
+
+void Engine::timer_end(KernelTimer &t) {
+  if (!t.enabled) return;
+  check(cudaEventRecord(t.pool[t.used].second, stream_), "timer record");
+  t.used++;
+  t.launches++;
+  if (t.used >= 512) {  // fold the finished pairs into the totals
+    check(cudaEventSynchronize(t.pool[t.used - 1].second), "timer sync");
+    for (size_t i = 0; i < t.used; ++i) {
+      float ms = 0;
+      check(cudaEventElapsedTime(&ms, t.pool[i].first, t.pool[i].second), "timer elapsed");
+      t.ms += ms;
+    }
+    t.used = 0;
+    t.bytes += t.pending_bytes;
+    t.pending_bytes = 0;
+  }
+}
+
+void Engine::set_kernel_timing(bool on) {
+  sync();
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_}) {
+    t->enabled = on;
+    t->used = 0;
+    t->launches = 0;
+    t->ms = t->bytes = t->pending_bytes = 0.0;
+  }
+}
+
+bool Engine::kernel_stats(const std::string &family, long *launches, double *ms, double *bytes) {
+  KernelTimer *t = nullptr;
+  if (family == "spmv") t = &t_spmv_;
+  else if (family == "cg_update") t = &t_update_;
+  else if (family == "assembly") t = &t_asm_;
+  else if (family == "residual") t = &t_res_;
+  if (!t) return false;
+  sync();
+  for (size_t i = 0; i < t->used; ++i) {
+    float m = 0;
+    check(cudaEventElapsedTime(&m, t->pool[i].first, t->pool[i].second), "timer elapsed");
+    t->ms += m;
+  }
+  t->used = 0;
+  t->bytes += t->pending_bytes;
+  t->pending_bytes = 0;
+  *launches = t->launches;
+  *ms = t->ms;
+  *bytes = t->bytes;
+  return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Batched solver pieces
+
+// assembly_rhs for the listed slots: out.norm and out.sig of each slot are valid afterwards.
+void Engine::residual(const std::vector<int> &slots) {
+  // Algorithmic bytes: u gathered once, history read once, b written once (element blocks stay in L2/HBM
+  // scratch and are not counted).
+  const double bytes = (double)slots.size() * (16.0 * nndim() + 8.0 * nvars());
+  timer_begin(t_res_, bytes);
+  launches_ += 2;
+  check_launch(mgb_launch_residual(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, (int)slots.size(), stream_),
+               "residual");
+  timer_end(t_res_);
+}
+
+// ell_solve_cgpd for the listed slots (b -> du); out.cg_its of each slot is valid afterwards.
+void Engine::cg_solve(const std::vector<int> &slots) {
+  const int n = (int)slots.size();
+  for (int s : slots) {
+    CgState c{};
+    c.min_err = cg_abs_tol_;
+    c.rel_err = cg_rel_tol_;
+    c.max_its = cg_max_its_;
+    check(cudaMemcpyAsync(slots_[s].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
+  }
+  launches_ += 2;
+  check_launch(mgb_launch_cg_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg setup");
+  // Algorithmic bytes per iteration and RVE (spmv): 81 values per row + x read + y written.
+  const double nrow = (double)nndim();
+  const double spmv_bytes = (double)n * nrow * (81.0 * 8 + 2.0 * 8);
+  const double upd_bytes = (double)n * nrow * 8.0 * 8;
+  const int chunk = (mesh_.nn > 200000) ? 8 : 32;
+  int done_its = 0;
+  while (done_its <= cg_max_its_) {
+    for (int it = 0; it < chunk; ++it) {
+      if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+      timer_begin(t_spmv_, spmv_bytes);
+      launches_ += 3;
+      check_launch(mgb_launch_cg_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg spmv");
+      timer_end(t_spmv_);
+      timer_begin(t_update_, upd_bytes);
+      check_launch(mgb_launch_cg_update(&mesh_, d_insts_, d_list_, n, stream_), "cg update");
+      timer_end(t_update_);
+      check_launch(mgb_launch_cg_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg p-update");
+    }
+    done_its += chunk;
+    check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
+    sync();
+    if (*h_count_ == 0) break;
+  }
+}
+
+// newton_raphson (solve.cpp:28-82) for a batch: slot s solves for strains[i] with its h_insts_ vars_old.
+// The per-slot state machine reproduces the reference loop exactly: a slot stops when its norm meets the
+// absolute or relative tolerance (checked before each iteration while its < nr_max_its), or after
+// nr_max_its iterations (then unconverged).
+std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
+                                         const std::vector<std::array<double, 6>> &strains) {
+  const int n = (int)slots.size();
+  std::vector<NewtonResult> res(n);
+  std::vector<double> norm0(n, 0.0), norm(n, 0.0);
+  std::vector<char> done(n, 0);
+  for (int i = 0; i < n; ++i) std::memcpy(h_insts_[slots[i]].strain, strains[i].data(), 6 * sizeof(double));
+  upload_insts();
+  upload_list(slots);
+  launches_ += 1;
+  check_launch(mgb_launch_set_bc(&mesh_, d_insts_, d_list_, n, stream_), "set_bc");
+  residual(slots);
+  download_out();
+  for (int i = 0; i < n; ++i) norm0[i] = norm[i] = h_out_[slots[i]].norm;
+  while (true) {
+    std::vector<int> active;
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i) {
+      if (done[i]) continue;
+      if (!(res[i].its < nr_max_its_)) {
+        done[i] = 1;
+        continue;
+      }
+      if (norm[i] < nr_max_tol_ || norm[i] < norm0[i] * nr_rel_tol_) {
+        res[i].converged = true;
+        done[i] = 1;
+        continue;
+      }
+      active.push_back(slots[i]);
+      idx.push_back(i);
+    }
+    if (active.empty()) break;
+    upload_list(active);
+    timer_begin(t_asm_, (double)active.size() * (8.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
+    launches_ += 9;
+    check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, (int)active.size(),
+                                     stream_),
+                 "assembly");
+    timer_end(t_asm_);
+    cg_solve(active);
+    launches_ += 1;
+    check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, (int)active.size(), stream_), "u += du");
+    residual(active);
+    download_out();
+    for (size_t a = 0; a < active.size(); ++a) {
+      const int i = idx[a];
+      const InstOut &o = h_out_[slots[i]];
+      res[i].solver_its += o.cg_its;
+      res[i].cg_maxed |= o.cg_maxed != 0;
+      total_cg_its_ += o.cg_its;
+      res[i].its++;
+      norm[i] = o.norm;
+    }
+  }
+  return res;
+}
+
+void Engine::allocate_vars(GpState &g) {
+  const size_t nv = nvars();
+  g.vars_n = dalloc<double>(nv, "vars_n");
+  g.vars_k = dalloc<double>(nv, "vars_k");
+  check(cudaMemsetAsync(g.vars_n, 0, nv * sizeof(double), stream_), "vars_n zero");
+  check(cudaMemsetAsync(g.vars_k, 0, nv * sizeof(double), stream_), "vars_k zero");
+  g.allocated = true;
+}
+
+// homogenize_fe_one_way / homogenize_fe_full (homogenize.cpp:111-282) for a batch of macro points.
+void Engine::homogenize_fe_batch(const std::vector<int> &gp_ids) {
+  const int n = (int)gp_ids.size();
+  const size_t ubytes = nndim() * sizeof(double);
+  std::vector<int> all(n);
+  for (int i = 0; i < n; ++i) all[i] = i;
+  std::vector<std::array<double, 6>> strains(n);
+  for (int i = 0; i < n; ++i) {
+    GpState &g = gps_[gp_ids[i]];
+    Slot &w = slots_[i];
+    Inst &I = h_insts_[i];
+    check(cudaMemcpyAsync(w.u, g.u_n, ubytes, cudaMemcpyDeviceToDevice, stream_), "u <- u_n");
+    I.vars_old = g.allocated ? g.vars_n : nullptr;
+    I.has_vars_old = g.allocated ? 1 : 0;
+    I.vars_new = g.allocated ? g.vars_k : w.vars_aux;
+    if (!g.allocated) check(cudaMemsetAsync(w.vars_aux, 0, nvars() * sizeof(double), stream_), "vars aux");
+    check(cudaMemsetAsync(w.out, 0, sizeof(InstOut), stream_), "out reset");
+    g.cost = 0;
+    g.subiterated = false;
+    g.status = 0;
+    std::memcpy(strains[i].data(), g.strain, sizeof(g.strain));
+  }
+  std::vector<NewtonResult> r = newton(all, strains);
+  std::vector<int> last_sits(n);
+  std::vector<int> unconv;
+  for (int i = 0; i < n; ++i) {
+    GpState &g = gps_[gp_ids[i]];
+    check(cudaMemcpyAsync(g.u_k, slots_[i].u, ubytes, cudaMemcpyDeviceToDevice, stream_), "u_k <- u");
+    g.nr_its = r[i].its;
+    g.nr_solver_its = r[i].solver_its;
+    g.nr_converged = r[i].converged;
+    g.cost += r[i].solver_its;
+    g.converged = r[i].converged;
+    if (r[i].cg_maxed) g.status |= MICROPP3_STATUS_CG_MAX_ITS;
+    last_sits[i] = r[i].solver_its;
+    if (!g.converged && subiterations_) unconv.push_back(i);
+  }
+
+  // Sub-iterations (homogenize.cpp:215-232): walk the increment again in nsubiterations steps from u_n.
+  if (!unconv.empty()) {
+    std::vector<std::array<double, 6>> eps_sub(unconv.size()), deps(unconv.size());
+    for (size_t a = 0; a < unconv.size(); ++a) {
+      GpState &g = gps_[gp_ids[unconv[a]]];
+      check(cudaMemcpyAsync(slots_[unconv[a]].u, g.u_n, ubytes, cudaMemcpyDeviceToDevice, stream_), "u <- u_n");
+      std::memcpy(eps_sub[a].data(), g.strain_old, sizeof(g.strain_old));
+      g.subiterated = true;
+      for (int v = 0; v < 6; ++v) deps[a][v] = (g.strain[v] - g.strain_old[v]) / nsubiterations_;
+    }
+    std::vector<NewtonResult> rs;
+    for (int it = 0; it < nsubiterations_; ++it) {
+      for (size_t a = 0; a < unconv.size(); ++a)
+        for (int v = 0; v < 6; ++v) eps_sub[a][v] += deps[a][v];
+      rs = newton(unconv, eps_sub);
+      for (size_t a = 0; a < unconv.size(); ++a) {
+        GpState &g = gps_[gp_ids[unconv[a]]];
+        g.cost += rs[a].solver_its;
+        if (rs[a].cg_maxed) g.status |= MICROPP3_STATUS_CG_MAX_ITS;
+        last_sits[unconv[a]] = rs[a].solver_its;
+      }
+    }
+    for (size_t a = 0; a < unconv.size(); ++a) {
+      GpState &g = gps_[gp_ids[unconv[a]]];
+      if (!rs.empty()) g.converged = rs[a].converged;
+      check(cudaMemcpyAsync(g.u_k, slots_[unconv[a]].u, ubytes, cudaMemcpyDeviceToDevice, stream_), "u_k <- u");
+    }
+  }
+
+  // Average stress from the last residual evaluation: it was made at u_k with vars_n.
+  download_out();
+  for (int i = 0; i < n; ++i) {
+    GpState &g = gps_[gp_ids[i]];
+    const InstOut &o = h_out_[i];
+    if (lin_stress_) {
+      std::memset(g.stress, 0, sizeof(g.stress));
+      for (int a = 0; a < 6; ++a)
+        for (int b = 0; b < 6; ++b) g.stress[a] += g.ctan[a * 6 + b] * g.strain[b];
+    } else {
+      std::memcpy(g.stress, o.sig, sizeof(g.stress));
+    }
+    if (!g.converged) g.status |= MICROPP3_STATUS_NEWTON_MAX_ITS;
+    if (o.nonfinite) g.status |= MICROPP3_STATUS_NONFINITE;
+  }
+
+  // calc_vars_new (update.cpp:32-56) at u_k = the slot's u.
+  for (int i = 0; i < n; ++i) check(cudaMemsetAsync(&slots_[i].out->nonlinear, 0, sizeof(int), stream_), "flag");
+  upload_insts();
+  upload_list(all);
+  launches_ += 1;
+  check_launch(mgb_launch_evolve(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "evolve");
+  download_out();
+  std::vector<int> pert;
+  for (int i = 0; i < n; ++i) {
+    GpState &g = gps_[gp_ids[i]];
+    if (h_out_[i].nonlinear && !g.allocated) {
+      allocate_vars(g);
+      check(cudaMemcpyAsync(g.vars_k, slots_[i].vars_aux, nvars() * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
+            "vars_k <- vars_new");
+    }
+    if (g.coupling == MICROPP3_FE_FULL && g.allocated) pert.push_back(i);
+  }
+
+  // ctan by 6 perturbed nonlinear solves (homogenize.cpp:256-275): u carried from u_k across the six
+  // solves, history vars_n, cost charged with the main solve's CG count each time.
+  if (!pert.empty()) {
+    std::vector<std::array<double, 6>> sig0(pert.size());
+    for (size_t a = 0; a < pert.size(); ++a) {
+      const int i = pert[a];
+      GpState &g = gps_[gp_ids[i]];
+      check(cudaMemcpyAsync(slots_[i].u, g.u_k, ubytes, cudaMemcpyDeviceToDevice, stream_), "u <- u_k");
+      h_insts_[i].vars_old = g.vars_n;
+      std::memcpy(sig0[a].data(), g.stress, sizeof(g.stress));
+    }
+    for (int c = 0; c < 6; ++c) {
+      std::vector<std::array<double, 6>> eps1(pert.size());
+      for (size_t a = 0; a < pert.size(); ++a) {
+        const GpState &g = gps_[gp_ids[pert[a]]];
+        std::memcpy(eps1[a].data(), g.strain, sizeof(g.strain));
+        eps1[a][c] += kDepsCtanAve;
+      }
+      std::vector<NewtonResult> rp = newton(pert, eps1);
+      for (size_t a = 0; a < pert.size(); ++a) {
+        const int i = pert[a];
+        GpState &g = gps_[gp_ids[i]];
+        g.cost += last_sits[i];
+        if (rp[a].cg_maxed) g.status |= MICROPP3_STATUS_CG_MAX_ITS;
+        const InstOut &o = h_out_[i];
+        for (int v = 0; v < 6; ++v) g.ctan[v * 6 + c] = (o.sig[v] - sig0[a][v]) / kDepsCtanAve;
+        if (o.nonfinite) g.status |= MICROPP3_STATUS_NONFINITE;
+      }
+    }
+  }
+  sync();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Public operations
+
+void Engine::set_strain(int gp, const double *strain) { std::memcpy(gps_.at(gp).strain, strain, 6 * sizeof(double)); }
+void Engine::get_stress(int gp, double *stress) const { std::memcpy(stress, gps_.at(gp).stress, 6 * sizeof(double)); }
+void Engine::get_ctan(int gp, double *ctan) const { std::memcpy(ctan, gps_.at(gp).ctan, 36 * sizeof(double)); }
+
+// homogenize (homogenize.cpp:68-99): linear points on the host, FE points batched on the GPU.
+void Engine::homogenize() {
+  check(cudaEventRecord(ev0_, stream_), "event");
+  std::vector<int> fe;
+  for (int i = 0; i < ngp_; ++i) {
+    GpState &g = gps_[i];
+    if (g.coupling == MICROPP3_FE_LINEAR || g.coupling == MICROPP3_MIX_RULE_CHAMIS) {
+      std::memset(g.stress, 0, sizeof(g.stress));
+      for (int a = 0; a < 6; ++a)
+        for (int b = 0; b < 6; ++b) g.stress[a] += g.ctan[a * 6 + b] * g.strain[b];
+    } else {
+      fe.push_back(i);
+    }
+  }
+  if (!fe.empty()) {
+    // Slots for as many points as memory allows (at most all of them).
+    size_t free_b = 0, total_b = 0;
+    check(cudaMemGetInfo(&free_b, &total_b), "mem info");
+    const double slot_bytes = 8.0 * (kEllPerNode * (double)mesh_.np + 8.0 * nndim() + 24.0 * mesh_.nelem + nvars());
+    const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes) + (int)slots_.size());
+    const int want = std::min((int)fe.size(), fit);
+    ensure_slots(want);
+    const int per = (int)slots_.size();
+    for (size_t b = 0; b < fe.size(); b += per) {
+      std::vector<int> part(fe.begin() + b, fe.begin() + std::min(fe.size(), b + per));
+      homogenize_fe_batch(part);
+    }
+  }
+  check(cudaEventRecord(ev1_, stream_), "event");
+  check(cudaEventSynchronize(ev1_), "event sync");
+  float ms = 0;
+  check(cudaEventElapsedTime(&ms, ev0_, ev1_), "elapsed");
+  last_ms_ = ms;
+}
+
+void Engine::homogenize_linear() {
+  for (auto &g : gps_) {
+    std::memset(g.stress, 0, sizeof(g.stress));
+    for (int a = 0; a < 6; ++a)
+      for (int b = 0; b < 6; ++b) g.stress[a] += g.ctan[a * 6 + b] * g.strain[b];
+  }
+}
+
+// update_vars (gp.hpp:95-105).
+void Engine::update_vars() {
+  for (auto &g : gps_) {
+    std::swap(g.vars_n, g.vars_k);
+    std::swap(g.u_n, g.u_k);
+    std::memcpy(g.strain_old, g.strain, sizeof(g.strain));
+  }
+}
+
+int Engine::get_non_linear_gps() const {
+  int c = 0;
+  for (const auto &g : gps_) c += g.allocated ? 1 : 0;
+  return c;
+}
+
+void Engine::get_newton(int gp, int *its, int *sits, int *conv) const {
+  const GpState &g = gps_.at(gp);
+  if (its) *its = g.nr_its;
+  if (sits) *sits = g.nr_solver_its;
+  if (conv) *conv = g.nr_converged ? 1 : 0;
+}
+
+// calc_ctan_lin_fe_models (micropp.cpp:255-284): 6 linear solves from u = 0 at strain 1e-8 e_i, batched.
+void Engine::calc_ctan_lin() {
+  size_t free_b = 0, total_b = 0;
+  check(cudaMemGetInfo(&free_b, &total_b), "mem info");
+  const double slot_bytes = 8.0 * (kEllPerNode * (double)mesh_.np + 8.0 * nndim() + 24.0 * mesh_.nelem + nvars());
+  const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes));
+  ensure_slots(std::min(6, fit));
+  const int per = (int)slots_.size();
+  for (int c0 = 0; c0 < 6; c0 += per) {
+    const int cnt = std::min(per, 6 - c0);
+    std::vector<int> sl(cnt);
+    std::vector<std::array<double, 6>> eps(cnt);
+    for (int a = 0; a < cnt; ++a) {
+      sl[a] = a;
+      eps[a].fill(0.0);
+      eps[a][c0 + a] += kDepsCtanAve;
+      check(cudaMemsetAsync(slots_[a].u, 0, nndim() * sizeof(double), stream_), "u zero");
+      h_insts_[a].vars_old = nullptr;
+      h_insts_[a].has_vars_old = 0;
+      h_insts_[a].vars_new = slots_[a].vars_aux;
+    }
+    newton(sl, eps);
+    download_out();
+    for (int a = 0; a < cnt; ++a)
+      for (int v = 0; v < 6; ++v) ctan_lin_[v * 6 + c0 + a] = h_out_[a].sig[v] / kDepsCtanAve;
+  }
+}
+
+void Engine::get_vars(int gp, int which, double *out) const {
+  const GpState &g = gps_.at(gp);
+  const double *src = g.allocated ? (which ? g.vars_k : g.vars_n) : nullptr;
+  if (src) {
+    check(cudaMemcpyAsync(out, src, nvars() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "vars download");
+    check(cudaStreamSynchronize(stream_), "sync");
+  } else {
+    std::memset(out, 0, nvars() * sizeof(double));
+  }
+}
+
+void Engine::get_u(int gp, int which, double *out) const {
+  const GpState &g = gps_.at(gp);
+  const double *src = which ? g.u_k : g.u_n;
+  if (src) {
+    check(cudaMemcpyAsync(out, src, nndim() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "u download");
+    check(cudaStreamSynchronize(stream_), "sync");
+  } else {
+    std::memset(out, 0, nndim() * sizeof(double));
+  }
+}
+
+void Engine::get_elem_type(int *out) const {
+  for (int e = 0; e < mesh_.nelem; ++e) out[e] = etype_[e];
+}
+
+void Engine::get_ctan_lin(double *out) const { std::memcpy(out, ctan_lin_, sizeof(ctan_lin_)); }
+
+static std::string restart_name(int rank, int id) {
+  std::ostringstream os;
+  os << "micropp-restart-" << rank << "-" << id << ".bin";
+  return os.str();
+}
+
+// write_restart (output.cpp:216-238, gp.hpp:107-113): per point a one-byte `allocated`, then vars_n and u_n.
+void Engine::write_restart(int restart_id) const {
+  std::ofstream f(restart_name(mpi_rank_, restart_id), std::ios::out | std::ios::binary);
+  if (!f) throw std::runtime_error("cannot open restart file for writing");
+  std::vector<double> vars(nvars()), u(nndim());
+  for (int i = 0; i < ngp_; ++i) {
+    const GpState &g = gps_[i];
+    const char a = g.allocated ? 1 : 0;
+    f.write(&a, 1);
+    if (g.allocated) {
+      get_vars(i, 0, vars.data());
+      get_u(i, 0, u.data());
+      f.write((const char *)vars.data(), vars.size() * sizeof(double));
+      f.write((const char *)u.data(), u.size() * sizeof(double));
+    }
+  }
+}
+
+// read_restart (output.cpp:240-262, gp.hpp:115-124): an allocated record brings vars_n and u_n back and
+// leaves vars_k zeroed.
+void Engine::read_restart(int restart_id) {
+  std::ifstream f(restart_name(mpi_rank_, restart_id), std::ios::in | std::ios::binary);
+  if (!f) throw std::runtime_error("cannot open restart file for reading");
+  std::vector<double> vars(nvars()), u(nndim());
+  for (int i = 0; i < ngp_; ++i) {
+    GpState &g = gps_[i];
+    char a = 0;
+    if (!f.read(&a, 1)) break;
+    if (a) {
+      if (!g.allocated) allocate_vars(g);
+      check(cudaMemsetAsync(g.vars_k, 0, nvars() * sizeof(double), stream_), "vars_k zero");
+      f.read((char *)vars.data(), vars.size() * sizeof(double));
+      f.read((char *)u.data(), u.size() * sizeof(double));
+      check(cudaMemcpyAsync(g.vars_n, vars.data(), vars.size() * sizeof(double), cudaMemcpyHostToDevice, stream_),
+            "vars_n upload");
+      if (g.u_n)
+        check(cudaMemcpyAsync(g.u_n, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "u_n");
+      sync();
+    } else if (g.allocated) {
+      dfree(g.vars_n);
+      dfree(g.vars_k);
+      g.vars_n = g.vars_k = nullptr;
+      g.allocated = false;
+    }
+  }
+  sync();
+}
+
+// print_info (micropp.cpp:546-597).
+void Engine::print_info() const {
+  static const char *names[] = {"MIC_HOMOGENEOUS", "MIC_SPHERE", "MIC_LAYER_Y", "MIC_CILI_FIB_X", "MIC_CILI_FIB_Z",
+                                "MIC_CILI_FIB_XZ", "MIC_QUAD_FIB_XYZ", "MIC_QUAD_FIB_XZ",
+                                "MIC_QUAD_FIB_XZ_BROKEN_X", "MIC3D_SPHERES", "MIC3D_8", "MIC3D_FIBS_20_ORDER",
+                                "MIC3D_FIBS_20_DISORDER"};
+  int count[4] = {0, 0, 0, 0};
+  for (const auto &g : gps_) count[g.coupling]++;
+  std::cout << "micropp3 (GB300)" << std::endl;
+  std::cout << "Micro-structure   : " << ((micro_type_ >= 0 && micro_type_ < 13) ? names[micro_type_] : "?") << std::endl;
+  std::cout << "MATRIX [%]        : " << Vm_ << std::endl;
+  std::cout << "FIBER  [%]        : " << Vf_ << std::endl;
+  std::cout << "FE_LINEAR         : " << count[0] << " GPs" << std::endl;
+  std::cout << "FE_ONE_WAY        : " << count[1] << " GPs" << std::endl;
+  std::cout << "FE_FULL           : " << count[2] << " GPs" << std::endl;
+  std::cout << "MIX_RULE_CHAMIS   : " << count[3] << " GPs" << std::endl;
+  std::cout << "NUM SUBITS        : " << nsubiterations_ << std::endl;
+  std::cout << "MPI RANK          : " << mpi_rank_ << std::endl;
+  std::cout << "ngp :" << ngp_ << " nx :" << mesh_.nx << " ny :" << mesh_.ny << " nz :" << mesh_.nz
+            << " nn :" << mesh_.nn << std::endl;
+  std::cout << "geo_params:";
+  for (double g : geo_params_) std::cout << " " << g;
+  std::cout << std::endl;
+  for (int i = 0; i < 3; ++i)
+    std::cout << "material " << i << ": type " << mats_.m[i].type << " E = " << mats_.m[i].E << " nu = " << mats_.m[i].nu
+              << " Ka = " << mats_.m[i].Ka << " Sy = " << mats_.m[i].Sy << " Xt = " << mats_.m[i].Xt << std::endl;
+  std::cout << std::endl << "ctan_lin_fe = " << std::endl;
+  for (int i = 0; i < 6; ++i) {
+    for (int j = 0; j < 6; ++j) std::cout << ctan_lin_[i * 6 + j] << "\t";
+    std::cout << std::endl;
+  }
+  std::cout << std::endl;
+}
+
+void Engine::output_vtu(int gp, const char *filename) {
+  (void)gp;
+  (void)filename;
+  throw std::runtime_error("VTU output is not available in this build");
+}
+
+}  // namespace mgb

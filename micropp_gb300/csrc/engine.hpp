@@ -1,0 +1,166 @@
+// engine.hpp -- host side of the GB300 homogenization: one Engine per micropp3 handle.
+//
+// The Engine owns the device state of every macro Gauss point of a handle (displacements u_n/u_k and the
+// internal variables vars_n/vars_k, mirroring gp_t, gp.hpp:33-125) and a pool of workspace slots.  A
+// homogenize() call runs all FE-coupled points of the handle through the solver at once: the slots of a
+// batch advance in lockstep through set_bc -> residual -> (assemble -> CG -> u += du -> residual)* with a
+// per-slot Newton mask, so each point sees exactly the reference's sequence of operations
+// (homogenize.cpp:188-282, solve.cpp:28-82) while every kernel launch covers the whole batch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "micropp_gb300.h"
+
+namespace mgb {
+
+struct GpState {
+  double strain_old[6] = {0, 0, 0, 0, 0, 0};
+  double strain[6] = {0, 0, 0, 0, 0, 0};
+  double stress[6] = {0, 0, 0, 0, 0, 0};
+  double ctan[36] = {0};
+  bool allocated = false;
+  long cost = 0;
+  bool converged = true;
+  bool subiterated = false;
+  int coupling = MICROPP3_FE_ONE_WAY;
+  int status = 0;
+  int nr_its = 0, nr_solver_its = 0;
+  bool nr_converged = false;
+  double *u_n = nullptr, *u_k = nullptr;        // device, nndim
+  double *vars_n = nullptr, *vars_k = nullptr;  // device, nvars (when allocated)
+};
+
+struct Slot {
+  double *u = nullptr, *du = nullptr, *b = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr;
+  double *kinv = nullptr, *vals = nullptr, *be = nullptr, *vars_aux = nullptr, *red = nullptr;
+  unsigned int *ticket = nullptr;
+  CgState *cg = nullptr;
+  InstOut *out = nullptr;
+};
+
+struct NewtonResult {
+  int its = 0, solver_its = 0;
+  bool converged = false;
+  bool cg_maxed = false;  // some CG solve of this Newton run stopped at cg_max_its
+};
+
+struct KernelTimer {
+  bool enabled = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+  size_t used = 0;
+  long launches = 0;
+  double ms = 0.0, bytes = 0.0, pending_bytes = 0.0;
+};
+
+class Engine {
+ public:
+  explicit Engine(const micropp3_config &cfg);
+  ~Engine();
+  Engine(const Engine &) = delete;
+  Engine &operator=(const Engine &) = delete;
+
+  int ngp() const { return ngp_; }
+  int nelem() const { return mesh_.nelem; }
+  int nndim() const { return mesh_.nn * 3; }
+  int nvars() const { return mesh_.nelem * kNpe * kNvarGp; }
+
+  void set_strain(int gp, const double *strain);
+  void get_stress(int gp, double *stress) const;
+  void get_ctan(int gp, double *ctan) const;
+  void homogenize();
+  void homogenize_linear();
+  void update_vars();
+
+  int is_non_linear(int gp) const { return gps_.at(gp).allocated ? 1 : 0; }
+  int get_non_linear_gps() const;
+  long get_cost(int gp) const { return gps_.at(gp).cost; }
+  bool has_converged(int gp) const { return gps_.at(gp).converged; }
+  bool has_subiterated(int gp) const { return gps_.at(gp).subiterated; }
+  int get_status(int gp) const { return gps_.at(gp).status; }
+  void get_newton(int gp, int *its, int *sits, int *conv) const;
+
+  void get_vars(int gp, int which, double *out) const;
+  void get_u(int gp, int which, double *out) const;
+  void get_elem_type(int *out) const;
+  void get_ctan_lin(double *out) const;
+  void write_restart(int restart_id) const;
+  void read_restart(int restart_id);
+  void output_vtu(int gp, const char *filename);
+  void print_info() const;
+
+  double last_homogenize_ms() const { return last_ms_; }
+  void set_kernel_timing(bool on);
+  bool kernel_stats(const std::string &family, long *launches, double *ms, double *bytes);
+  long total_cg_its() const { return total_cg_its_; }
+  long kernel_launches() const { return launches_; }
+  int mpi_rank() const { return mpi_rank_; }
+
+ private:
+  // setup
+  void build_mesh(const micropp3_config &cfg);
+  void build_elem_types(const micropp3_config &cfg);
+  void build_materials(const micropp3_config &cfg);
+  void build_phase_stiffness();
+  void ensure_slots(int n);
+  void free_slots();
+  void calc_ctan_lin();
+  void ctan_mix_rule_chamis(double *ctan) const;
+
+  // batched solver pieces (slot indices)
+  void upload_insts();
+  void upload_list(const std::vector<int> &slots);
+  void download_out();
+  void residual(const std::vector<int> &slots);
+  void cg_solve(const std::vector<int> &slots);
+  std::vector<NewtonResult> newton(const std::vector<int> &slots, const std::vector<std::array<double, 6>> &strains);
+  void homogenize_fe_batch(const std::vector<int> &gp_ids);
+  void allocate_vars(GpState &g);
+  void timer_begin(KernelTimer &t, double bytes);
+  void timer_end(KernelTimer &t);
+  void sync();
+
+  int ngp_ = 0;
+  int micro_type_ = 0;
+  int mpi_rank_ = 0;
+  double geo_params_[4] = {0, 0, 0, 0};
+  struct material_base mat_in_[3];
+  int nr_max_its_ = 4, cg_max_its_ = 1000;
+  double nr_max_tol_ = 1e-10, nr_rel_tol_ = 1e-3, cg_abs_tol_ = 1e-50, cg_rel_tol_ = 1e-5;
+  bool lin_stress_ = true, subiterations_ = false, calc_ctan_lin_ = true;
+  int nsubiterations_ = 10;
+  int precision_ = 0, ctan_mode_ = 0;
+
+  MeshDev mesh_{};
+  Mats mats_{};
+  double bmat_[8][6][24];
+  double dsh_[8 * 24];
+  double ke_phase_[3][576];
+  std::vector<int8_t> etype_;
+  double Vm_ = 0, Vf_ = 0;
+  double ctan_lin_[36] = {0};
+  std::vector<GpState> gps_;
+
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  int8_t *d_etype_ = nullptr;
+  double *d_dsh_ = nullptr, *d_ke_ = nullptr;
+  std::vector<Slot> slots_;
+  std::vector<Inst> h_insts_;
+  Inst *d_insts_ = nullptr;
+  int *d_list_ = nullptr;
+  int list_cap_ = 0;
+  InstOut *h_out_ = nullptr;  // pinned mirror of the slots' out records
+  unsigned int *d_count_ = nullptr, *h_count_ = nullptr;
+  double last_ms_ = 0.0;
+  long total_cg_its_ = 0;
+  long launches_ = 0;  // kernels of this library launched by the handle
+  KernelTimer t_spmv_, t_update_, t_asm_, t_res_;
+};
+
+}  // namespace mgb

@@ -1,0 +1,412 @@
+// fe_kernels.cu -- finite-element kernels of the FP64 homogenization path (sm_103a).
+//
+// Every kernel runs over a batch: blockIdx.y indexes the list of active instances, blockIdx.x tiles the
+// nodes or elements of one RVE.  Summation orders follow the reference where a sum is local (Gauss points of
+// an element, elements around a node); only grid-wide reductions use a tree.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "launch.h"
+#include "laws.cuh"
+#include "reduce.cuh"
+
+namespace mgb {
+
+// Local hex8 corner (ox,oy,oz) -> local node index (common.cpp:28-40 numbering).
+__device__ __forceinline__ int local_of(int ox, int oy, int oz) { return oz * 4 + (oy ? 3 - ox : ox); }
+__device__ __constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                             {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+__device__ __forceinline__ bool is_boundary(const MeshDev &m, int i, int j, int k) {
+  return i == 0 || j == 0 || k == 0 || i == m.nx - 1 || j == m.ny - 1 || k == m.nz - 1;
+}
+
+// strain = B(gp) * u_e with the non-zero terms in the reference's order (common.cpp:57-72).
+// dsh: the 8 nodal gradients at this Gauss point, dsh[a*3 + d].
+__device__ __forceinline__ void gp_strain(const double *dsh, const double *ue, double *eps) {
+  double e0 = 0, e1 = 0, e2 = 0, e3 = 0, e4 = 0, e5 = 0;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const double gx = dsh[a * 3], gy = dsh[a * 3 + 1], gz = dsh[a * 3 + 2];
+    const double ux = ue[a * 3], uy = ue[a * 3 + 1], uz = ue[a * 3 + 2];
+    e0 += gx * ux;
+    e1 += gy * uy;
+    e2 += gz * uz;
+    e3 += gy * ux;
+    e3 += gx * uy;
+    e4 += gz * ux;
+    e4 += gx * uz;
+    e5 += gz * uy;
+    e5 += gy * uz;
+  }
+  eps[0] = e0; eps[1] = e1; eps[2] = e2; eps[3] = e3; eps[4] = e4; eps[5] = e5;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Affine displacement boundary condition u = eps_t x on the six faces (micro3D.cpp:26-78).  A node on
+// several faces takes the coordinates of the last face written by the reference (x=lx, then x=0, y=ly,
+// y=0, z=lz, z=0 in decreasing priority).
+__global__ void k_set_bc(MeshDev m, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const int i = n % m.nx, j = (n / m.nx) % m.ny, k = n / m.nxny;
+  if (!is_boundary(m, i, j, k)) return;
+  double c[3];
+  if (i == m.nx - 1) {
+    c[0] = m.lx; c[1] = j * m.dy; c[2] = k * m.dz;
+  } else if (i == 0) {
+    c[0] = 0; c[1] = j * m.dy; c[2] = k * m.dz;
+  } else if (j == m.ny - 1) {
+    c[0] = i * m.dx; c[1] = m.ly; c[2] = k * m.dz;
+  } else if (j == 0) {
+    c[0] = i * m.dx; c[1] = 0; c[2] = k * m.dz;
+  } else if (k == m.nz - 1) {
+    c[0] = i * m.dx; c[1] = j * m.dy; c[2] = m.lz;
+  } else {
+    c[0] = i * m.dx; c[1] = j * m.dy; c[2] = 0;
+  }
+  const double *e = I.strain;
+  const double et[3][3] = {{e[0], 0.5 * e[3], 0.5 * e[4]}, {0.5 * e[3], e[1], 0.5 * e[5]}, {0.5 * e[4], 0.5 * e[5], e[2]}};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double t = 0.0;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) t += et[a][b] * c[b];
+    I.u[n * 3 + a] = t;
+  }
+}
+
+// u += du over all unknowns (solve.cpp:73).
+__global__ void k_add_du(int nndim, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x) I.u[t] += I.du[t];
+}
+
+// dst = src for the listed instances; src/dst selected by `which` (0: u <- u_n, 1: u_k <- u).
+__global__ void k_copy(int n, const double *const *src, double *const *dst, const int *list) {
+  const int y = list[blockIdx.y];
+  const double *s = src[y];
+  double *d = dst[y];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) d[t] = s[t];
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Element residual blocks be = sum_gp B^T sigma(B u_e, vars) wg (assembly.cpp:123-138), one thread per
+// element, plus the element's share of the volume average of sigma (average.cpp:57-82), reduced over the
+// grid into out.sig.
+__global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, const int8_t *etype,
+                                                           const double *dsh_g, const Inst *insts,
+                                                           const int *list) {
+  __shared__ double dsh[8 * 24];
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
+  __syncthreads();
+  const Inst &I = insts[list[blockIdx.y]];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double aux[6] = {0, 0, 0, 0, 0, 0};
+  if (e < m.nelem) {
+    const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
+    const int n0 = ez * m.nxny + ey * m.nx + ex;
+    double ue[24];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ue[a * 3 + d] = I.u[n * 3 + d];
+    }
+    const MatDev &mat = mats.m[etype[e]];
+    double be[24];
+#pragma unroll
+    for (int i = 0; i < 24; ++i) be[i] = 0.0;
+    const double wg = m.wg;
+#pragma unroll 1
+    for (int g = 0; g < 8; ++g) {
+      const double *dg = &dsh[g * 24];
+      double eps[6], s[6];
+      gp_strain(dg, ue, eps);
+      law_stress(mat, eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr, s);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+        be[a * 3 + 0] += gx * s[0] * wg;
+        be[a * 3 + 0] += gy * s[3] * wg;
+        be[a * 3 + 0] += gz * s[4] * wg;
+        be[a * 3 + 1] += gy * s[1] * wg;
+        be[a * 3 + 1] += gx * s[3] * wg;
+        be[a * 3 + 1] += gz * s[5] * wg;
+        be[a * 3 + 2] += gz * s[2] * wg;
+        be[a * 3 + 2] += gx * s[4] * wg;
+        be[a * 3 + 2] += gy * s[5] * wg;
+      }
+#pragma unroll
+      for (int v = 0; v < 6; ++v) aux[v] += s[v] * wg;
+    }
+#pragma unroll
+    for (int i = 0; i < 24; ++i) I.be[(size_t)i * m.nelem + e] = be[i];
+  }
+  double tot[6];
+  const int nb = gridDim.x;
+  if (grid_sum<6>(aux, I.red, I.ticket, nb, tot) && threadIdx.x == 0) {
+    bool bad = false;
+#pragma unroll
+    for (int v = 0; v < 6; ++v) {
+      I.out->sig[v] = tot[v] / m.vol_tot;
+      bad |= !isfinite(tot[v]);
+    }
+    if (bad) I.out->nonfinite = 1;
+  }
+}
+
+// Node gather of the residual: b = -(sum of the element blocks of the 8 elements around the node, in the
+// reference's element order ez, ey, ex), zero on Dirichlet rows (assembly.cpp:27-103), and ||b||_2.
+__global__ void __launch_bounds__(kNodeBlock) k_node_rhs(MeshDev m, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  double sq[1] = {0.0};
+  if (n < m.nn) {
+    const int i = n % m.nx, j = (n / m.nx) % m.ny, k = n / m.nxny;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    if (!is_boundary(m, i, j, k)) {
+#pragma unroll
+      for (int dz = -1; dz <= 0; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 0; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 0; ++dx) {
+            const int e = ((k + dz) * m.ney + (j + dy)) * m.nex + (i + dx);
+            const int a = local_of(-dx, -dy, -dz);
+            b0 += I.be[(size_t)(a * 3 + 0) * m.nelem + e];
+            b1 += I.be[(size_t)(a * 3 + 1) * m.nelem + e];
+            b2 += I.be[(size_t)(a * 3 + 2) * m.nelem + e];
+          }
+      b0 = -b0;
+      b1 = -b1;
+      b2 = -b2;
+    }
+    I.b[n * 3 + 0] = b0;
+    I.b[n * 3 + 1] = b1;
+    I.b[n * 3 + 2] = b2;
+    sq[0] = b0 * b0 + b1 * b1 + b2 * b2;
+  }
+  double tot[1];
+  if (grid_sum<1>(sq, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+    I.out->norm = sqrt(tot[0]);
+    if (!isfinite(tot[0])) I.out->nonfinite = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Jacobian assembly into ELL (assembly.cpp:105-178, ell-common.cpp:166-198).
+//
+// Elements are processed in 8 colours (parity of ex, ey, ez) so that two elements of one launch never share
+// a node: each launch adds its elements' 24x24 blocks into the rows of their interior nodes without atomics,
+// and the order in which a matrix entry receives its (up to 8) contributions is fixed.  A block holds
+// kMatElems elements x 24 threads; thread p of an element owns row p of its Ke.
+//
+// Nonlinear laws: per Gauss point the tangent C (FD, 7 stress evaluations) is formed by 8 threads, then
+// cxb = (C B) wg is built cooperatively in shared memory and each thread accumulates its row
+// Ke[p][:] += B[:,p]^T cxb -- the reference's association (assembly.cpp:159-176).  Elastic-law elements
+// scatter the phase's precomputed Ke (identical for every element of a phase: B and wg are uniform).
+constexpr int kMatElems = 8;
+
+__device__ __forceinline__ int ell_idx(int s, int fi, int fj) { return s * 9 + fi * 3 + fj; }
+
+__global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mats, const int8_t *etype,
+                                                              const double *dsh_g, const double *ke_phase,
+                                                              const Inst *insts, const int *list, int color) {
+  __shared__ double dsh[8 * 24];
+  __shared__ double ue[kMatElems][24];
+  __shared__ double Cg[kMatElems][8][36];
+  __shared__ double cxb[kMatElems][6 * 24];
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
+  const Inst &I = insts[list[blockIdx.y]];
+  const int cx = color & 1, cy = (color >> 1) & 1, cz = (color >> 2) & 1;
+  const int ncx = (m.nex - cx + 1) / 2, ncy = (m.ney - cy + 1) / 2, ncz = (m.nez - cz + 1) / 2;
+  const int nce = ncx * ncy * ncz;
+  const int el = threadIdx.x / 24, p = threadIdx.x % 24;
+  const int ce = blockIdx.x * kMatElems + el;
+  const bool valid = ce < nce;
+  int ex = 0, ey = 0, ez = 0, e = 0, n0 = 0, law = 0, ph = 0;
+  if (valid) {
+    ex = 2 * (ce % ncx) + cx;
+    ey = 2 * ((ce / ncx) % ncy) + cy;
+    ez = 2 * (ce / (ncx * ncy)) + cz;
+    e = (ez * m.ney + ey) * m.nex + ex;
+    n0 = ez * m.nxny + ey * m.nx + ex;
+    ph = etype[e];
+    law = mats.m[ph].type;
+    const int a = p / 3, d = p % 3;
+    const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+    ue[el][p] = I.u[n * 3 + d];
+  }
+  __syncthreads();
+  const bool nonlin = valid && law != 0;
+  // Gauss-point tangents.
+  if (nonlin && p < 8) {
+    double eps[6];
+    gp_strain(&dsh[p * 24], ue[el], eps);
+    law_ctan(mats.m[ph], eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr, Cg[el][p]);
+  }
+  __syncthreads();
+  double row[24];
+  const int a = p / 3, d = p % 3;
+  // Non-zero rows m of column p of B in ascending order, and their coefficients.
+  const int m0 = d, m1 = (d == 0) ? 3 : (d == 1 ? 3 : 4), m2 = (d == 0) ? 4 : 5;
+  if (nonlin) {
+#pragma unroll
+    for (int q = 0; q < 24; ++q) row[q] = 0.0;
+  } else if (valid) {
+    const double *K = ke_phase + (size_t)ph * 576 + p * 24;
+#pragma unroll
+    for (int q = 0; q < 24; ++q) row[q] = K[q];
+  }
+#pragma unroll 1
+  for (int g = 0; g < 8; ++g) {
+    const double *dg = &dsh[g * 24];
+    // B column p has B[m0][p], B[m1][p], B[m2][p] non-zero.
+    const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+    const double bp0 = (d == 0) ? gx : (d == 1 ? gy : gz);
+    const double bp1 = (d == 0) ? gy : gx;
+    const double bp2 = (d == 0) ? gz : (d == 1 ? gz : gy);
+    if (nonlin) {
+      // cxb[mm][p] = wg * sum_k C[mm][k] B[k][p] over the non-zero k of column p (ascending).
+      const double *C = Cg[el][g];
+#pragma unroll
+      for (int mm = 0; mm < 6; ++mm) {
+        double t = 0.0;
+        t += C[mm * 6 + m0] * bp0;
+        t += C[mm * 6 + m1] * bp1;
+        t += C[mm * 6 + m2] * bp2;
+        cxb[el][mm * 24 + p] = t * m.wg;
+      }
+    }
+    __syncthreads();
+    if (nonlin) {
+#pragma unroll
+      for (int q = 0; q < 24; ++q) {
+        row[q] += bp0 * cxb[el][m0 * 24 + q];
+        row[q] += bp1 * cxb[el][m1 * 24 + q];
+        row[q] += bp2 * cxb[el][m2 * 24 + q];
+      }
+    }
+    __syncthreads();
+  }
+  if (!valid) return;
+  // Scatter row p = (local node a, dof d) into the ELL row of node(a), unless it is a boundary row.
+  const int ai = c_corner[a][0], aj = c_corner[a][1], ak = c_corner[a][2];
+  const int gi = ex + ai, gj = ey + aj, gk = ez + ak;
+  if (is_boundary(m, gi, gj, gk)) return;
+  const int node = n0 + ak * m.nxny + aj * m.nx + ai;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const int s = (c_corner[b][2] - ak + 1) * 9 + (c_corner[b][1] - aj + 1) * 3 + (c_corner[b][0] - ai + 1);
+#pragma unroll
+    for (int fj = 0; fj < 3; ++fj) {
+      double *dst = &I.vals[(size_t)ell_idx(s, d, fj) * m.np + node];
+      *dst += row[b * 3 + fj];
+    }
+  }
+}
+
+// Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
+__global__ void k_zero_vals(size_t count, const Inst *insts, const int *list) {
+  double *v = insts[list[blockIdx.y]].vals;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
+    v[t] = 0.0;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Internal-variable update (update.cpp:32-56), one thread per Gauss point; the nonlinear flags are OR-ed
+// into out.nonlinear.
+__global__ void __launch_bounds__(kNodeBlock) k_evolve(MeshDev m, Mats mats, const int8_t *etype,
+                                                         const double *dsh_g, const Inst *insts,
+                                                         const int *list) {
+  __shared__ double dsh[8 * 24];
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
+  __syncthreads();
+  const Inst &I = insts[list[blockIdx.y]];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool nl = false;
+  if (t < m.nelem * 8) {
+    const int e = t >> 3, g = t & 7;
+    const MatDev &mat = mats.m[etype[e]];
+    if (mat.type != 0) {
+      const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
+      const int n0 = ez * m.nxny + ey * m.nx + ex;
+      double ue[24], eps[6];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ue[a * 3 + d] = I.u[n * 3 + d];
+      }
+      gp_strain(&dsh[g * 24], ue, eps);
+      const size_t off = ((size_t)e * 8 + g) * kNvarGp;
+      nl = law_evolve(mat, eps, I.has_vars_old ? I.vars_old + off : nullptr, I.has_vars_old != 0, I.vars_new + off);
+    }
+  }
+  if (__syncthreads_or(nl) && threadIdx.x == 0) atomicOr(&I.out->nonlinear, 1);
+}
+
+}  // namespace mgb
+
+// ---------------------------------------------------------------------------------------------------
+// Launch wrappers (the C-ABI layer the host engine calls).
+
+using namespace mgb;
+
+static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+extern "C" {
+
+int mgb_launch_set_bc(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_set_bc<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_add_du(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const int nndim = m->nn * 3;
+  k_add_du<<<dim3(cdiv(nndim, 4 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(nndim, insts, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_copy(int n, const double *const *src, double *const *dst, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_copy<<<dim3(cdiv(n, 4 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(n, src, dst, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_residual(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
+                        const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_elem_rhs<<<dim3(cdiv(m->nelem, kElemBlock), nlist), kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
+  k_node_rhs<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
+                        const double *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const size_t count = (size_t)kEllPerNode * m->np;
+  k_zero_vals<<<dim3(cdiv(count, 8 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(count, insts, list);
+  for (int c = 0; c < 8; ++c) {
+    const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
+    const int nce = ((m->nex - cx + 1) / 2) * ((m->ney - cy + 1) / 2) * ((m->nez - cz + 1) / 2);
+    if (nce <= 0) continue;
+    k_elem_mat<<<dim3(cdiv(nce, kMatElems), nlist), kMatElems * 24, 0, s>>>(*m, *mats, etype, dsh, ke_phase,
+                                                                            insts, list, c);
+  }
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_evolve(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
+                      const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_evolve<<<dim3(cdiv((size_t)m->nelem * 8, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, *mats, etype, dsh, insts,
+                                                                                     list);
+  return (int)cudaGetLastError();
+}
+
+}  // extern "C"

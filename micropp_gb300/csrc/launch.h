@@ -1,0 +1,35 @@
+// launch.h -- the internal C-ABI layer between the host engine (C++) and the CUDA kernels.
+//
+// Every entry launches one stage of the homogenization over a batch of instances on a stream and returns
+// the cudaError_t of the launch (0 on success).  `insts` is a device array of per-instance views, `list` a
+// device array of the `nlist` instance indices that take part.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "device.cuh"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int mgb_launch_set_bc(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_add_du(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_copy(int n, const double *const *src, double *const *dst, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_residual(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                        const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_assembly(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                        const double *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_evolve(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                      const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
+                          unsigned int *active_count, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif

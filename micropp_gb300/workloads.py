@@ -1,0 +1,70 @@
+"""Seeded synthetic RVE inputs of the benchmark and parity cases.
+
+The reference's micro types do not include the two microstructures of these workloads, so they are given as
+element phase maps (``micropp3_config.elem_type``), the way a caller of the library would:
+
+* ``layers_z(n)``   -- 4 parallel stiff layers normal to z, 0.1 thick, centred at z = .125, .375, .625,
+  .875 (phase 1 where |z_centroid - c| < 0.05, else 0);
+* ``spheres(n, k, r, seed)`` -- k non-overlapping spheres of radius r with seeded uniform centres
+  (rejection sampling, fully inside the cube), phase 1 inside.
+
+Material parameters follow the damage-law mapping recorded in the design doc: the reference damage law has a
+single threshold parameter Xt (material.cpp:227-268) and a hard-wired softening table, so the damage
+matrix uses Xt ~ U[1e5, 3e5] per RVE (smaller Xt fully damages Gauss points and the reference itself
+returns NaN stresses).
+"""
+import numpy as np
+
+
+def centroids(n):
+    c = (np.arange(n) + 0.5) / n
+    return c
+
+
+def layers_z(n, centres=(0.125, 0.375, 0.625, 0.875), half_width=0.05):
+    """Phase map (nelem,) int32 in glo_elem order (ez slowest)."""
+    zc = centroids(n)
+    lay = np.zeros(n, dtype=bool)
+    for c in centres:
+        lay |= np.abs(zc - c) < half_width
+    et = np.zeros((n, n, n), dtype=np.int32)
+    et[lay, :, :] = 1
+    return et.reshape(-1)
+
+
+def sphere_centres(k, r, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    tries = 0
+    while len(out) < k:
+        tries += 1
+        if tries > 100000:
+            raise RuntimeError("could not place non-overlapping spheres")
+        c = rng.uniform(r, 1 - r, size=3)
+        if all(np.linalg.norm(c - o) >= 2 * r for o in out):
+            out.append(c)
+    return np.array(out)
+
+
+def spheres(n, k=8, r=0.12, seed=0):
+    cs = sphere_centres(k, r, seed)
+    c = centroids(n)
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    inside = np.zeros_like(x, dtype=bool)
+    for cc in cs:
+        inside |= (x - cc[0]) ** 2 + (y - cc[1]) ** 2 + (z - cc[2]) ** 2 < r * r
+    return inside.astype(np.int32).reshape(-1)
+
+
+def damage_thresholds(count, seed, lo=1e5, hi=3e5):
+    return np.random.default_rng(seed).uniform(lo, hi, size=count)
+
+
+def monotone_path(target, steps):
+    """Strain at steps 1..steps toward `target` (6,)."""
+    target = np.asarray(target, dtype=np.float64)
+    return [target * (s / steps) for s in range(1, steps + 1)]
+
+
+def random_targets(count, seed, amp):
+    return np.random.default_rng(seed).uniform(-amp, amp, size=(count, 6))

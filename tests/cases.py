@@ -1,0 +1,53 @@
+"""Parity cases: the same seeded inputs for the GB300 library and for the oracle."""
+import numpy as np
+
+import pyoracle as orc
+from micropp_gb300 import workloads as wl
+
+ELASTIC, PLASTIC, DAMAGE = 0, 1, 2
+
+
+def oracle_config(n, ngp=1, micro_type=0, geo=(0.1, 0.1, 0.1, 0.1), mats=((0, 1e7, 0.25, 0, 0, 0),) * 3,
+                  coupling=None, elem_type=None, **kw):
+    return orc.make_config(n, ngp=ngp, micro_type=micro_type, geo=geo,
+                           mats=[orc.material(*m) for m in mats], coupling=coupling, elem_type=elem_type, **kw)
+
+
+def gpu_config(n, ngp=1, micro_type=0, geo=(0.1, 0.1, 0.1, 0.1), mats=((0, 1e7, 0.25, 0, 0, 0),) * 3,
+               coupling=None, elem_type=None, **kw):
+    import micropp_gb300 as mg
+    return mg.config(n, ngp=ngp, micro_type=micro_type, geo=geo, mats=[mg.material(*m) for m in mats],
+                     coupling=coupling, elem_type=elem_type, **kw)
+
+
+def case(name):
+    """Named parity cases: (kwargs for both configs, list of per-step strain lists per GP)."""
+    if name == "c1_sphere_elastic":
+        # 10^3 elements, centred sphere r=0.2, both phases elastic, eps_xx = 1e-3.
+        kw = dict(n=10, micro_type=1, geo=(0.2, 0, 0, 0),
+                  mats=((0, 1e7, 0.25, 0, 0, 0), (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0)),
+                  coupling=[2], lin_stress=0, nr_max_tol=1e-5)
+        steps = [[np.array([1e-3, 0, 0, 0, 0, 0])]]
+        return kw, steps
+    if name == "damage_layers":
+        n = 8
+        kw = dict(n=n, ngp=2, elem_type=wl.layers_z(n),
+                  mats=((2, 1e7, 0.25, 0, 0, 1e5), (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0)),
+                  coupling=[2, 2], lin_stress=0, nr_max_its=12, nr_max_tol=1e-5)
+        base = np.array([2e-2, -0.3 * 2e-2, 0, 0.5 * 2e-2, 0, 0])
+        steps = [[base * s / 3, 0.6 * base * s / 3] for s in range(1, 4)]
+        return kw, steps
+    if name == "plastic_sphere":
+        n = 6
+        kw = dict(n=n, micro_type=1, geo=(0.2, 0, 0, 0),
+                  mats=((1, 1e7, 0.3, 1e5, 1e4, 0), (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0)),
+                  coupling=[2], lin_stress=0, nr_max_its=30, nr_max_tol=1e-5)
+        steps = [[np.array([1e-2, 0, 0, 0, 0, 0]) * s / 4] for s in range(1, 5)]
+        return kw, steps
+    raise KeyError(name)
+
+
+def split_kw(kw):
+    kw = dict(kw)
+    n = kw.pop("n")
+    return n, kw

@@ -1,0 +1,100 @@
+"""Generate the golden fixtures of tests/golden/ from the reference (run where the reference tree exists).
+
+1. benchmark_tables.json -- the known-answer tables of the reference's own tests
+   test/benchmark-{elastic,plastic,damage}.cpp (sig_sol[10][6], tolerance, material), parsed from those
+   files, together with the outputs of the compiled reference (oracle/_ref) on the same 10-step paths.
+2. ref_<case>.npz -- outputs of the compiled reference on the seeded parity cases of tests/cases.py:
+   per step and Gauss point the average stress, ctan, cost, flags, and the internal variables and the
+   displacement of the last step.
+
+Usage: python tests/golden/make_golden.py [reference_root]   (needs oracle/build_ref.sh to have run)
+"""
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import pyoracle as orc  # noqa: E402
+
+
+def parse_table(path):
+    text = open(path).read()
+    body = re.search(r"sig_sol\[time_steps\]\[6\]\s*=\s*\{(.*?)\};", text, flags=re.S).group(1)
+    rows = re.findall(r"\{([^{}]*)\}", body)
+    sig = [[float(x) for x in r.split(",")] for r in rows]
+    tol = float(re.search(r"fabs\(sig_sol\[t\]\[i\] - sig\[i\]\) < ([0-9.eE+-]+)\)", text).group(1))
+    m = re.search(r"material_set\(&mic_params\.materials\[0\],\s*([^)]*)\)", text).group(1)
+    vals = [float(x) for x in m.split(",")]
+    material = [int(vals[0])] + vals[1:]
+    return sig, tol, material
+
+
+def run_table_case(material):
+    cfg = orc.make_config(1, mats=[orc.material(*material), orc.material(0, 3e7, 0.25), orc.material(0, 3e7, 0.25)],
+                          lin_stress=0)
+    r = orc.RefRVE(cfg)
+    out = []
+    t = 0.0
+    for _ in range(10):
+        eps = np.zeros(6)
+        eps[0] = 0.1 * t
+        r.set_strain(0, eps)
+        r.homogenize()
+        out.append(r.get_stress(0).tolist())
+        r.update_vars()
+        t += 0.015
+    r.close()
+    return out
+
+
+def run_case(name):
+    from cases import case, oracle_config, split_kw
+    kw, steps = case(name)
+    n, kw2 = split_kw(kw)
+    r = orc.RefRVE(oracle_config(n, **kw2))
+    rec = {"stress": [], "ctan": [], "cost": [], "converged": [], "nonlinear": []}
+    for st in steps:
+        for gp, e in enumerate(st):
+            r.set_strain(gp, e)
+        r.homogenize()
+        ng = len(st)
+        rec["stress"].append([r.get_stress(g) for g in range(ng)])
+        rec["ctan"].append([r.get_ctan(g) for g in range(ng)])
+        rec["cost"].append([r.get_cost(g) for g in range(ng)])
+        rec["converged"].append([r.has_converged(g) for g in range(ng)])
+        rec["nonlinear"].append([r.is_non_linear(g) for g in range(ng)])
+        last_vars = [r.vars(g, 1) for g in range(ng)]
+        last_u = [r.u(g, 1) for g in range(ng)]
+        r.update_vars()
+    arrays = {k: np.array(v) for k, v in rec.items()}
+    arrays["vars_k_last"] = np.array(last_vars)
+    arrays["u_k_last"] = np.array(last_u)
+    arrays["ctan_lin"] = r.ctan_lin()
+    r.close()
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **arrays)
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    tables = {}
+    for key in ("elastic", "plastic", "damage"):
+        sig, tol, material = parse_table(os.path.join(ref, "test", f"benchmark-{key}.cpp"))
+        tables[key] = {"source": f"test/benchmark-{key}.cpp", "sig": sig, "tol": tol, "material": material,
+                       "ref_output": run_table_case(material)}
+    with open(os.path.join(HERE, "benchmark_tables.json"), "w") as f:
+        json.dump(tables, f, indent=1)
+    for name in ("c1_sphere_elastic", "damage_layers", "plastic_sphere"):
+        run_case(name)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,124 @@
+"""Pin the oracle (C restatement) to the reference: its own golden tables, the committed fixtures made by
+the compiled reference, and -- where the reference tree is built here -- live bit-for-bit comparisons."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle as orc
+from cases import case, oracle_config, split_kw
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def table_run(material):
+    cfg = orc.make_config(1, mats=[orc.material(*material), orc.material(0, 3e7, 0.25), orc.material(0, 3e7, 0.25)],
+                          lin_stress=0)
+    r = orc.OracleRVE(cfg)
+    out, t = [], 0.0
+    for _ in range(10):
+        eps = np.zeros(6)
+        eps[0] = 0.1 * t
+        r.set_strain(0, eps)
+        r.homogenize()
+        out.append(r.get_stress(0))
+        r.update_vars()
+        t += 0.015
+    return np.array(out)
+
+
+@pytest.mark.parametrize("key", ["elastic", "plastic", "damage"])
+def test_reference_golden_tables(key):
+    """test/benchmark-{elastic,plastic,damage}.cpp known answers, at the tests' own tolerances."""
+    g = json.load(open(os.path.join(GOLD, "benchmark_tables.json")))[key]
+    sig = table_run(g["material"])
+    assert np.max(np.abs(sig - np.array(g["sig"]))) < g["tol"]
+    assert np.array_equal(sig, np.array(g["ref_output"]))  # bit-for-bit with the compiled reference
+
+
+@pytest.mark.parametrize("name", ["c1_sphere_elastic", "damage_layers", "plastic_sphere"])
+def test_reference_fixtures(name):
+    """Seeded FE_FULL cases: stress, ctan, cost, flags, history and displacement equal the reference's."""
+    ref = np.load(os.path.join(GOLD, f"ref_{name}.npz"))
+    kw, steps = case(name)
+    n, kw2 = split_kw(kw)
+    r = orc.OracleRVE(oracle_config(n, **kw2))
+    assert np.array_equal(r.ctan_lin(), ref["ctan_lin"])
+    for s, st in enumerate(steps):
+        for gp, e in enumerate(st):
+            r.set_strain(gp, e)
+        r.homogenize()
+        for gp in range(len(st)):
+            assert np.array_equal(r.get_stress(gp), ref["stress"][s][gp])
+            assert np.array_equal(r.get_ctan(gp), ref["ctan"][s][gp])
+            assert r.get_cost(gp) == ref["cost"][s][gp]
+            assert r.has_converged(gp) == ref["converged"][s][gp]
+            assert r.is_non_linear(gp) == ref["nonlinear"][s][gp]
+            if s == len(steps) - 1:
+                assert np.array_equal(r.vars(gp, 1), ref["vars_k_last"][gp])
+                assert np.array_equal(r.u(gp, 1), ref["u_k_last"][gp])
+        r.update_vars()
+
+
+needs_ref = pytest.mark.skipif(not orc.ref_available(), reason="compiled reference (oracle/_ref) not built here")
+
+
+@needs_ref
+@pytest.mark.parametrize("micro", list(range(13)))
+def test_live_micro_types(micro):
+    """Element phases and the linear ctan of every reference micro type (n = 6)."""
+    geo = (0.2, 0.2, 0.2, 0.2)
+    mats = [orc.material(0, 1e7, 0.25), orc.material(0, 1e8, 0.25), orc.material(0, 5e7, 0.3)]
+    cfg = orc.make_config(6, micro_type=micro, geo=geo, mats=mats)
+    a, b = orc.OracleRVE(cfg), orc.RefRVE(cfg)
+    assert np.array_equal(a.elem_type(), b.elem_type())
+    assert np.array_equal(a.vol_fractions(), b.vol_fractions())
+    assert np.array_equal(a.ctan_lin(), b.ctan_lin())
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [1, 2])
+def test_live_random_paths(seed):
+    """Random strain paths on damage and J2 matrices with several Gauss points, incl. a mixture-rule point
+    and sub-iterations (forced by nr_max_its = 2)."""
+    rng = np.random.default_rng(seed)
+    law = [(2, 1e7, 0.25, 0, 0, 1e5), (1, 1e7, 0.3, 1e5, 1e4, 0)][seed % 2]
+    mats = [orc.material(*law), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    cfg = orc.make_config(5, ngp=3, micro_type=1, geo=(0.25, 0, 0, 0), mats=mats, coupling=[2, 1, 3],
+                          lin_stress=0, nr_max_its=2, subiterations=1, nsubiterations=3)
+    a, b = orc.OracleRVE(cfg), orc.RefRVE(cfg)
+    for step in range(3):
+        for gp in range(3):
+            e = rng.uniform(-1.5e-2, 1.5e-2, 6)
+            a.set_strain(gp, e)
+            b.set_strain(gp, e)
+        a.homogenize()
+        b.homogenize()
+        for gp in range(3):
+            assert np.array_equal(a.get_stress(gp), b.get_stress(gp))
+            assert np.array_equal(a.get_ctan(gp), b.get_ctan(gp))
+            assert a.get_cost(gp) == b.get_cost(gp)
+            assert a.has_converged(gp) == b.has_converged(gp)
+            assert a.has_subiterated(gp) == b.has_subiterated(gp)
+            assert np.array_equal(a.vars(gp, 1), b.vars(gp, 1))
+        a.update_vars()
+        b.update_vars()
+
+
+@needs_ref
+def test_live_restart_format(tmp_path, monkeypatch):
+    """Restart files: byte-identical to the reference's micropp-restart-<rank>-<id>.bin."""
+    monkeypatch.chdir(tmp_path)
+    mats = [orc.material(2, 1e7, 0.25, 0, 0, 1e5), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    cfg = orc.make_config(4, ngp=2, micro_type=1, geo=(0.25, 0, 0, 0), mats=mats, coupling=[2, 2], lin_stress=0,
+                          nr_max_its=12)
+    a, b = orc.OracleRVE(cfg), orc.RefRVE(cfg)
+    for r in (a, b):
+        r.set_strain(0, [3e-2, 0, 0, 0, 0, 0])
+        r.set_strain(1, [1e-4, 0, 0, 0, 0, 0])
+        r.homogenize()
+        r.update_vars()
+    b.write_restart(7)
+    a.write_restart(str(tmp_path / "oracle.bin"))
+    assert (tmp_path / "micropp-restart-0-7.bin").read_bytes() == (tmp_path / "oracle.bin").read_bytes()
