@@ -2,8 +2,7 @@
 """RVE homogenizations/s (stress + ctan) at 60^3 on one GB300.
 
 Workload (default): R = 32 damage RVEs of 60^3 elements (226,981 nodes, 680,943 DOF each): 4 stiff layers
-normal to z (E = 1e8, nu = 0.25, 0.1 thick), damage matrix (E = 1e7, nu = 0.25, Xt ~ U[1e5, 3e5] per RVE,
-seeded), FE_FULL coupling with lin_stress off, Newton <= 12 iterations at tolerance 1e-5, DPCG at the
+normal to z (E = 1e8, nu = 0.25, 0.1 thick), damage matrix (E = 1e7, nu = 0.25, Xt = 1e5), FE_FULL coupling with lin_stress off, Newton <= 12 iterations at tolerance 1e-5, DPCG at the
 reference's 1e-5.  Each RVE has a seeded macro strain target ~ U[-2.5e-2, 2.5e-2]^6 (scaled up until the
 RVE is nonlinear).  Set-up loads every RVE to half its target and accepts the step; a bench step is one
 macro iteration: every RVE is homogenized (stress and ctan: one Newton solve plus six perturbed solves) at
@@ -43,7 +42,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--n", type=int, default=60, help="elements per axis")
+    p.add_argument("--size", type=int, default=60, help="elements per axis")
     p.add_argument("--rves", type=int, default=32, help="RVEs per GPU")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample-rves", type=int, default=0, help="RVEs in the CPU sample (default: host cores)")
@@ -55,8 +54,14 @@ def parse():
 # workload
 
 def workload(n, rves, seed, rank):
+    """Phase map, damage thresholds and strain targets of the RVEs of one rank.
+
+    The reference's damage law is continuous at first loading only for Xt = 1e5, its hard-wired Ey
+    (material.cpp:205-268): a larger Xt makes the stress jump by q(r)/r (5x at Xt = 2.35e5) and a smaller
+    one fully damages points (NaN).  Every RVE therefore uses Xt = 1e5; the RVEs differ by their seeded
+    strain targets."""
     from micropp_gb300 import workloads as wl
-    xts = wl.damage_thresholds(rves, seed + 1000 * rank)
+    xts = np.full(rves, 1e5)
     targets = wl.random_targets(rves, seed + 1000 * rank + 1, 2.5e-2)
     return wl.layers_z(n), xts, targets
 
@@ -118,16 +123,15 @@ class ClockSampler:
 
 def cpu_sample(n, xts, targets, cores):
     """Times one Newton iteration (1 residual, 1 assembly, 1 DPCG solve, 1 residual) of `cores` RVEs of the
-    workload in parallel on the oracle, at the same preloaded state as the GPU arm's first Newton iteration
-    is not reproduced exactly: the sample starts from u = 0 at half the target strain.  Returns
-    (seconds, CG iterations summed over the sample RVEs)."""
+    workload in parallel on the oracle, starting from u = 0 at half the target strain.  Returns (seconds, CG
+    iterations summed over the sample RVEs)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as orc
     from micropp_gb300 import workloads as wl
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     et = wl.layers_z(n)
-    # one handle per distinct Xt is needed for exact materials; the sample uses the first RVE's Xt for all
-    # `cores` points so the reference's own OpenMP loop over Gauss points (homogenize.cpp:72) runs them.
+    # All RVEs share the materials, so one handle with `cores` Gauss points holds the sample and the
+    # reference's own OpenMP loop over Gauss points (homogenize.cpp:72) runs them in parallel.
     mats = [orc.material(2, 1e7, 0.25, 0, 0, float(xts[0])), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
     cfg = orc.make_config(n, ngp=cores, mats=mats, coupling=[1] * cores, elem_type=et, lin_stress=0, nr_max_its=1,
                           nr_max_tol=1e-5, calc_ctan_lin=0)
@@ -140,6 +144,27 @@ def cpu_sample(n, xts, targets, cores):
     its = sum(r.newton(gp)[1] for gp in range(cores))
     r.close()
     return dt, its
+
+
+def cpu_cg_its_per_homogenization(n, xts, targets):
+    """CG iterations of one full stress+ctan homogenization of the first RVE of the workload, on the oracle
+    (affordable only for small n)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as orc
+    from micropp_gb300 import workloads as wl
+    mats = [orc.material(2, 1e7, 0.25, 0, 0, float(xts[0])), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    r = orc.OracleRVE(orc.make_config(n, coupling=[2], elem_type=wl.layers_z(n), mats=mats, lin_stress=0,
+                                      nr_max_its=12, nr_max_tol=1e-5, calc_ctan_lin=0))
+    r.set_strain(0, 0.5 * targets[0])
+    r.homogenize()
+    r.update_vars()
+    r.set_strain(0, targets[0])
+    r.homogenize()
+    # cost counts the main solve's CG iterations 7 times (homogenize.cpp:269); the Newton record has the
+    # main solve alone, so the perturbed solves are estimated as 6 x main.
+    its = r.newton(0)[1]
+    r.close()
+    return 7.0 * max(its, 1)
 
 
 def host_cores():
@@ -183,9 +208,11 @@ def run_reference(args):
     if rank != 0:
         return
     cores = host_cores()
-    n = args.n
+    n = args.size
     _, xts, targets = workload(n, args.rves, args.seed, 0)
     per_hom = CG_ITS_PER_HOM.get(n)
+    if per_hom is None and n <= 24:
+        per_hom = cpu_cg_its_per_homogenization(n, xts, targets)
     if per_hom is None:
         print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable":
                           f"no measured CG-iterations-per-homogenization figure for n={n}"}))
@@ -234,7 +261,7 @@ def run_gpu(args):
     if world > 1:
         import torch
         torch.cuda.set_device(local)
-    n, R = args.n, args.rves
+    n, R = args.size, args.rves
     et, xts, targets = workload(n, R, args.seed, rank)
     handles = []
     for i in range(R):
@@ -321,7 +348,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{R} damage RVEs of {n}^3 per GPU (4 layers normal to z, Xt~U[1e5,3e5]), "
+        "config": {"workload": f"{R} damage RVEs of {n}^3 per GPU (4 layers normal to z, Xt=1e5), "
                                f"FE_FULL stress+ctan (1 + 6 perturbed Newton solves), plain FP64 form",
                    "n": n, "rves_per_gpu": R, "form": "plain-fp64", "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (441 MB ELL per RVE)", "nonlinear_rves": nonlinear},

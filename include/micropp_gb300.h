@@ -109,6 +109,20 @@ void micropp3_set_kernel_timing(struct micropp3 *self, int enable);
 int micropp3_kernel_stats(const struct micropp3 *self, const char *family, long *launches, double *ms,
                           double *bytes);
 
+/* Jacobi-preconditioned CG on a stencil ELL matrix held in device memory; the counterpart of the reference's
+ * ell_solve_cgpd (ell.hpp:63, ell.cpp:66-122): x0 = 0, stop when ||z|| < abs_tol or ||z|| < rel_tol * ||z0||,
+ * or after max_its iterations; *its receives the iteration count.  The work vectors are allocated on the
+ * device for the duration of the call.
+ *   nodes  grid of nodes nx, ny, nz (3 unknowns per node, nrow = 3 nx ny nz)
+ *   vals   243 * np doubles, np = nx ny nz rounded up to a multiple of 32: entry (s, fi, fj) of node n at
+ *          vals[(s*9 + fi*3 + fj) * np + n], stencil slot s = 9 (dz+1) + 3 (dy+1) + (dx+1) for the neighbour
+ *          at offset (dx, dy, dz).  Rows of boundary nodes are identity rows; their entries are not read.
+ *   b, x   nrow doubles, node-interleaved (row = 3 n + d)
+ *   stream a cudaStream_t (NULL: the default stream)
+ * Returns 0, -1 for invalid arguments, or the CUDA error code. */
+int micropp3_ell_solve_cgpd(const int nodes[3], const double *vals, const double *b, double *x, double rel_tol,
+                            double abs_tol, int max_its, int *its, void *stream);
+
 /* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
 long micropp3_total_cg_its(const struct micropp3 *self);
 long micropp3_kernel_launches(const struct micropp3 *self);

@@ -110,6 +110,8 @@ def load():
         "micropp3_total_cg_its": (C.c_long, [H]),
         "micropp3_kernel_launches": (C.c_long, [H]),
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
+        "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                             C.c_int, ip, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

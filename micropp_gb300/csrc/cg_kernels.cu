@@ -197,7 +197,7 @@ int mgb_launch_cg_spmv(const MeshDev *m, const Inst *insts, const int *list, int
 
 int mgb_launch_cg_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg_update<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock * 4), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg_update<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
@@ -205,7 +205,7 @@ int mgb_launch_cg_update(const MeshDev *m, const Inst *insts, const int *list, i
 int mgb_launch_cg_pupdate(const MeshDev *m, const Inst *insts, const int *list, int nlist, unsigned int *active_count,
                           cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg_pupdate<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock * 4), nlist), kNodeBlock, 0, s>>>(*m, insts, list,
+  k_cg_pupdate<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list,
                                                                                          active_count);
   return (int)cudaGetLastError();
 }

@@ -12,6 +12,9 @@
 //                                            implicit; boundary rows are identity rows and are not stored.
 //   element residual blocks be               24 * nelem doubles, [(a*3+d) * nelem + e]
 //   internal variables                       7 doubles per Gauss point, [(e*8 + g)*7 + v] (params.hpp:41)
+// Mixed form: the same ELL layout in FP32 (vals32) with FP32 CG vectors; the six tangent right-hand sides
+// of the implicit ctan are stored node-major, [(n*6 + i)*3 + d] (18 values per node), so one thread reads a
+// node's 6 x 3 block contiguously.
 #pragma once
 
 #include <stdint.h>
@@ -52,14 +55,26 @@ struct CgState {
   int its, max_its, done, pad;
 };
 
+// Per-instance scalars of the 6-RHS tangent CG (one independent CG per right-hand side).
+struct Cg6State {
+  double rz[6], pnorm0[6], pnorm[6], alpha[6], beta[6];
+  double min_err, rel_err;
+  int its, max_its, done[6], all_done, pad;
+};
+
 // Small per-instance outputs read back by the host.
 struct InstOut {
   double norm;         // ||b||_2 of the last residual evaluation
   double sig[6];       // volume-averaged stress of the last residual evaluation
+  double ctan[36];     // implicit ctan (row-major, column i = d sigma / d eps_i)
+  double res6[6];      // ||f_i - K x_i|| of the last tangent refinement residual
+  double f6[6];        // ||f_i|| of the tangent right-hand sides
   int cg_its;          // iterations of the last CG solve
   int nonlinear;       // OR of the evolute flags of the last update pass
   int nonfinite;       // a reduction produced NaN/Inf
   int cg_maxed;        // the last CG solve stopped at max_its
+  int cg6_its;         // iterations of the last 6-RHS CG solve
+  int pad;
 };
 
 struct Inst {
@@ -70,12 +85,18 @@ struct Inst {
   unsigned int *ticket;    // last-block counter for the reductions
   CgState *cg;
   InstOut *out;
+  // mixed form (FP32 Jacobian and CG vectors)
+  float *vals32, *kinv32, *r32, *z32, *p32, *Ap32, *du32;
+  // implicit ctan: 6 right-hand sides
+  double *X6, *F6;
+  float *R6, *Z6, *P6, *AP6, *D6;
+  Cg6State *cg6;
   double strain[6];
   int has_vars_old;        // J2 evolute writes only when a history buffer exists (material.cpp:168-181)
   int pad;
 };
 
-constexpr int kRedStride = 8;
+constexpr int kRedStride = 40;
 constexpr int kNodeBlock = 256;
 constexpr int kElemBlock = 128;
 

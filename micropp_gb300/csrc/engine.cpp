@@ -25,6 +25,12 @@ namespace {
 constexpr double kConstXg = 0.577350269189626;  // params.hpp:34
 constexpr double kDepsCtanAve = 1.0e-8;        // params.hpp:32
 
+// Tangent solve of the implicit ctan: FP32 CG sweeps to this relative tolerance, refined with FP64 residuals
+// until ||f_i - K x_i|| <= kTangentTol ||f_i|| for all six right-hand sides (at most kTangentSweeps sweeps).
+constexpr double kTangentSweepRel = 1.0e-5;
+constexpr double kTangentTol = 1.0e-9;
+constexpr int kTangentSweeps = 4;
+
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
 void check(cudaError_t e, const char *what) {
@@ -73,9 +79,10 @@ Engine::Engine(const micropp3_config &cfg) {
   calc_ctan_lin_ = cfg.calc_ctan_lin != 0;
   precision_ = cfg.precision;
   ctan_mode_ = cfg.ctan_mode;
-  if (precision_ != MICROPP3_FP64) throw std::invalid_argument("this build serves precision = MICROPP3_FP64 only");
-  if (ctan_mode_ != MICROPP3_CTAN_PERTURB)
-    throw std::invalid_argument("this build serves ctan_mode = MICROPP3_CTAN_PERTURB only");
+  if (precision_ != MICROPP3_FP64 && precision_ != MICROPP3_MIXED)
+    throw std::invalid_argument("precision must be MICROPP3_FP64 or MICROPP3_MIXED");
+  if (ctan_mode_ != MICROPP3_CTAN_PERTURB && ctan_mode_ != MICROPP3_CTAN_IMPLICIT)
+    throw std::invalid_argument("ctan_mode must be MICROPP3_CTAN_PERTURB or MICROPP3_CTAN_IMPLICIT");
 
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
@@ -95,6 +102,12 @@ Engine::Engine(const micropp3_config &cfg) {
   check(cudaMemcpy(d_dsh_, dsh_, sizeof(dsh_), cudaMemcpyHostToDevice), "dsh upload");
   d_ke_ = dalloc<double>(3 * 576, "ke");
   check(cudaMemcpy(d_ke_, ke_phase_, sizeof(ke_phase_), cudaMemcpyHostToDevice), "ke upload");
+  {
+    float ke32[3 * 576];
+    for (int i = 0; i < 3 * 576; ++i) ke32[i] = (float)(&ke_phase_[0][0])[i];
+    d_ke32_ = dalloc<float>(3 * 576, "ke32");
+    check(cudaMemcpy(d_ke32_, ke32, sizeof(ke32), cudaMemcpyHostToDevice), "ke32 upload");
+  }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
 
@@ -146,7 +159,7 @@ Engine::~Engine() {
     dfree(g.vars_k);
   }
   free_slots();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_})
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_})
     for (auto &e : t->pool) {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
@@ -154,6 +167,7 @@ Engine::~Engine() {
   dfree(d_etype_);
   dfree(d_dsh_);
   dfree(d_ke_);
+  dfree(d_ke32_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -325,32 +339,67 @@ void Engine::ctan_mix_rule_chamis(double *ctan) const {
 // ------------------------------------------------------------------------------------------------
 // Workspace slots
 
+// Device bytes of one workspace slot in this handle's mode.
+double Engine::slot_bytes() const {
+  const double nd = nndim(), np = mesh_.np;
+  double b = 8.0 * (3.0 * nd + 24.0 * mesh_.nelem + nvars());  // u, du, b, be, vars_aux
+  if (precision_ == MICROPP3_FP64) b += 8.0 * (kEllPerNode * np + 5.0 * nd);
+  if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 4.0 * kEllPerNode * np;
+  if (precision_ == MICROPP3_MIXED) b += 4.0 * 6.0 * nd;
+  if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 8.0 * 2.0 * 6.0 * nd + 4.0 * 5.0 * 6.0 * nd;
+  return b;
+}
+
 void Engine::ensure_slots(int n) {
   if ((int)slots_.size() >= n) return;
   const int old = (int)slots_.size();
   const size_t nd = nndim(), nv = nvars();
-  const int nblocks = std::max((mesh_.nn + kNodeBlock - 1) / kNodeBlock, (mesh_.nelem + kElemBlock - 1) / kElemBlock) + 8;
+  // Reduction partials: one slot per block of the largest reducing grid (the row-parallel CG updates,
+  // 3*nn/kNodeBlock blocks; the Gauss-point kernels, 8*nelem/128 blocks).
+  const int nblocks = std::max((3 * mesh_.nn + kNodeBlock - 1) / kNodeBlock, (mesh_.nelem * 8 + 127) / 128) + 8;
+  const bool fp64 = precision_ == MICROPP3_FP64, mixed = precision_ == MICROPP3_MIXED;
+  const bool implicit = ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
   slots_.resize(n);
   for (int s = old; s < n; ++s) {
     Slot &w = slots_[s];
     w.u = dalloc<double>(nd, "u");
     w.du = dalloc<double>(nd, "du");
     w.b = dalloc<double>(nd, "b");
-    w.r = dalloc<double>(nd, "r");
-    w.z = dalloc<double>(nd, "z");
-    w.p = dalloc<double>(nd, "p");
-    w.Ap = dalloc<double>(nd, "Ap");
-    w.kinv = dalloc<double>(nd, "kinv");
-    w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
     w.be = dalloc<double>((size_t)24 * mesh_.nelem, "element residuals");
     w.vars_aux = dalloc<double>(nv, "vars_new_aux");
     w.red = dalloc<double>((size_t)nblocks * kRedStride, "partials");
     w.ticket = dalloc<unsigned int>(1, "ticket");
     w.cg = dalloc<CgState>(1, "cg state");
     w.out = dalloc<InstOut>(1, "out");
+    if (fp64) {
+      w.r = dalloc<double>(nd, "r");
+      w.z = dalloc<double>(nd, "z");
+      w.p = dalloc<double>(nd, "p");
+      w.Ap = dalloc<double>(nd, "Ap");
+      w.kinv = dalloc<double>(nd, "kinv");
+      w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
+    }
+    if (mixed || implicit) w.vals32 = dalloc<float>((size_t)kEllPerNode * mesh_.np, "ELL values (FP32)");
+    if (mixed) {
+      w.kinv32 = dalloc<float>(nd, "kinv32");
+      w.r32 = dalloc<float>(nd, "r32");
+      w.z32 = dalloc<float>(nd, "z32");
+      w.p32 = dalloc<float>(nd, "p32");
+      w.Ap32 = dalloc<float>(nd, "Ap32");
+      w.du32 = dalloc<float>(nd, "du32");
+    }
+    if (implicit) {
+      w.X6 = dalloc<double>(6 * nd, "X6");
+      w.F6 = dalloc<double>(6 * nd, "F6");
+      w.R6 = dalloc<float>(6 * nd, "R6");
+      w.Z6 = dalloc<float>(6 * nd, "Z6");
+      w.P6 = dalloc<float>(6 * nd, "P6");
+      w.AP6 = dalloc<float>(6 * nd, "AP6");
+      w.D6 = dalloc<float>(6 * nd, "D6");
+      w.cg6 = dalloc<Cg6State>(1, "cg6 state");
+    }
     check(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), stream_), "ticket");
     check(cudaMemsetAsync(w.out, 0, sizeof(InstOut), stream_), "out");
-    check(cudaMemsetAsync(w.p, 0, nd * sizeof(double), stream_), "p");
   }
   dfree(d_insts_);
   d_insts_ = dalloc<Inst>(n, "insts");
@@ -362,6 +411,9 @@ void Engine::ensure_slots(int n) {
     Inst &I = h_insts_[s];
     I.u = w.u; I.du = w.du; I.b = w.b; I.r = w.r; I.z = w.z; I.p = w.p; I.Ap = w.Ap; I.kinv = w.kinv;
     I.vals = w.vals; I.be = w.be; I.red = w.red; I.ticket = w.ticket; I.cg = w.cg; I.out = w.out;
+    I.vals32 = w.vals32; I.kinv32 = w.kinv32; I.r32 = w.r32; I.z32 = w.z32; I.p32 = w.p32; I.Ap32 = w.Ap32;
+    I.du32 = w.du32;
+    I.X6 = w.X6; I.F6 = w.F6; I.R6 = w.R6; I.Z6 = w.Z6; I.P6 = w.P6; I.AP6 = w.AP6; I.D6 = w.D6; I.cg6 = w.cg6;
     I.vars_old = nullptr;
     I.vars_new = w.vars_aux;
   }
@@ -374,9 +426,12 @@ void Engine::ensure_slots(int n) {
 
 void Engine::free_slots() {
   for (auto &w : slots_) {
-    for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red}) dfree(p);
+    for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red, w.X6, w.F6})
+      dfree(p);
+    for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6}) dfree(p);
     dfree(w.ticket);
     dfree(w.cg);
+    dfree(w.cg6);
     dfree(w.out);
   }
   slots_.clear();
@@ -441,7 +496,7 @@ void Engine::timer_end(KernelTimer &t) {
 
 void Engine::set_kernel_timing(bool on) {
   sync();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_}) {
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_}) {
     t->enabled = on;
     t->used = 0;
     t->launches = 0;
@@ -455,6 +510,7 @@ bool Engine::kernel_stats(const std::string &family, long *launches, double *ms,
   else if (family == "cg_update") t = &t_update_;
   else if (family == "assembly") t = &t_asm_;
   else if (family == "residual") t = &t_res_;
+  else if (family == "spmv6") t = &t_spmv6_;
   if (!t) return false;
   sync();
   for (size_t i = 0; i < t->used; ++i) {
@@ -523,13 +579,142 @@ void Engine::cg_solve(const std::vector<int> &slots) {
   }
 }
 
+// The mixed form's CG: FP32 values and vectors, FP64 dot products, same iteration and stop rule.
+void Engine::cg_solve32(const std::vector<int> &slots) {
+  const int n = (int)slots.size();
+  for (int s : slots) {
+    CgState c{};
+    c.min_err = cg_abs_tol_;
+    c.rel_err = cg_rel_tol_;
+    c.max_its = cg_max_its_;
+    check(cudaMemcpyAsync(slots_[s].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
+  }
+  launches_ += 1;
+  check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
+  const double nrow = (double)nndim();
+  const double spmv_bytes = (double)n * nrow * (81.0 * 4 + 2.0 * 4);
+  const double upd_bytes = (double)n * nrow * 8.0 * 4;
+  const int chunk = (mesh_.nn > 200000) ? 8 : 32;
+  int done_its = 0;
+  while (done_its <= cg_max_its_) {
+    for (int it = 0; it < chunk; ++it) {
+      if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+      timer_begin(t_spmv_, spmv_bytes);
+      launches_ += 3;
+      check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg32 spmv");
+      timer_end(t_spmv_);
+      timer_begin(t_update_, upd_bytes);
+      check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
+      timer_end(t_update_);
+      check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
+    }
+    done_its += chunk;
+    check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
+    sync();
+    if (*h_count_ == 0) break;
+  }
+}
+
+// Implicit ctan of the listed slots at their current u with their vars_old: assemble the FP32 tangent, form
+// the six right-hand sides, solve with refined FP32 CG sweeps, average.  out.ctan of each slot is valid
+// afterwards.  Returns the CG iterations each slot spent.
+std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
+  const int n = (int)slots.size();
+  std::vector<int> its(n, 0);
+  upload_insts();
+  upload_list(slots);
+  timer_begin(t_asm_, (double)n * (4.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
+  launches_ += 9;
+  check_launch(mgb_launch_assembly32(&mesh_, &mats_, d_etype_, d_dsh_, d_ke32_, d_insts_, d_list_, n, stream_),
+               "tangent assembly");
+  timer_end(t_asm_);
+  launches_ += 1;
+  check_launch(mgb_launch_t6_rhs(&mesh_, d_insts_, d_list_, n, stream_), "tangent rhs");
+  const double nrow = (double)nndim();
+  const double spmv_bytes = (double)n * nrow * (81.0 * 4 + 2.0 * 6 * 4);
+  const int chunk = (mesh_.nn > 200000) ? 8 : 32;
+  std::vector<int> live = slots;
+  std::vector<int> live_idx(n);
+  for (int i = 0; i < n; ++i) live_idx[i] = i;
+  for (int sweep = 0; sweep < kTangentSweeps && !live.empty(); ++sweep) {
+    for (int s : live) {
+      Cg6State c{};
+      c.min_err = 0.0;
+      c.rel_err = kTangentSweepRel;
+      c.max_its = cg_max_its_;
+      check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
+    }
+    if (sweep > 0) upload_list(live);
+    launches_ += 1;
+    check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), stream_), "tangent residual");
+    download_out();
+    std::vector<int> next, next_idx;
+    for (size_t a = 0; a < live.size(); ++a) {
+      const InstOut &o = h_out_[live[a]];
+      bool ok = true;
+      for (int r = 0; r < 6; ++r) ok &= o.res6[r] <= kTangentTol * o.f6[r];
+      if (!ok && std::isfinite(o.res6[0])) {
+        next.push_back(live[a]);
+        next_idx.push_back(live_idx[a]);
+      }
+    }
+    if (next.size() != live.size()) {
+      // Converged slots leave; the CG states of the others were initialised by the residual kernel.
+      live = next;
+      live_idx = next_idx;
+      if (live.empty()) break;
+      upload_list(live);
+      for (int s : live) {
+        Cg6State c{};
+        c.min_err = 0.0;
+        c.rel_err = kTangentSweepRel;
+        c.max_its = cg_max_its_;
+        check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
+      }
+      launches_ += 1;
+      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), stream_), "tangent residual");
+    }
+    const int nl = (int)live.size();
+    int done_its = 0;
+    while (done_its <= cg_max_its_) {
+      for (int it = 0; it < chunk; ++it) {
+        if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+        timer_begin(t_spmv6_, spmv_bytes * nl / n);
+        launches_ += 3;
+        check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 spmv");
+        timer_end(t_spmv6_);
+        check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");
+        check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
+      }
+      done_its += chunk;
+      check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
+      sync();
+      if (*h_count_ == 0) break;
+    }
+    launches_ += 1;
+    check_launch(mgb_launch_t6_accumulate(&mesh_, d_insts_, d_list_, nl, stream_), "tangent accumulate");
+    download_out();
+    for (size_t a = 0; a < live.size(); ++a) {
+      its[live_idx[a]] += h_out_[live[a]].cg6_its;
+      total_cg_its_ += h_out_[live[a]].cg6_its;
+    }
+  }
+  upload_list(slots);
+  launches_ += 1;
+  check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
+  download_out();
+  return its;
+}
+
 // newton_raphson (solve.cpp:28-82) for a batch: slot s solves for strains[i] with its h_insts_ vars_old.
 // The per-slot state machine reproduces the reference loop exactly: a slot stops when its norm meets the
 // absolute or relative tolerance (checked before each iteration while its < nr_max_its), or after
-// nr_max_its iterations (then unconverged).
+// nr_max_its iterations (then unconverged).  In the mixed form the Jacobian and its CG are FP32 while the
+// residual that decides convergence stays FP64.
 std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
                                          const std::vector<std::array<double, 6>> &strains) {
   const int n = (int)slots.size();
+  const bool mixed = precision_ == MICROPP3_MIXED;
   std::vector<NewtonResult> res(n);
   std::vector<double> norm0(n, 0.0), norm(n, 0.0);
   std::vector<char> done(n, 0);
@@ -560,15 +745,24 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     }
     if (active.empty()) break;
     upload_list(active);
-    timer_begin(t_asm_, (double)active.size() * (8.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
+    const int na = (int)active.size();
+    timer_begin(t_asm_, (double)na * ((mixed ? 4.0 : 8.0) * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
     launches_ += 9;
-    check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, (int)active.size(),
-                                     stream_),
-                 "assembly");
+    if (mixed)
+      check_launch(mgb_launch_assembly32(&mesh_, &mats_, d_etype_, d_dsh_, d_ke32_, d_insts_, d_list_, na, stream_),
+                   "assembly");
+    else
+      check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, na, stream_),
+                   "assembly");
     timer_end(t_asm_);
-    cg_solve(active);
     launches_ += 1;
-    check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, (int)active.size(), stream_), "u += du");
+    if (mixed) {
+      cg_solve32(active);
+      check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+    } else {
+      cg_solve(active);
+      check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+    }
     residual(active);
     download_out();
     for (size_t a = 0; a < active.size(); ++a) {
@@ -694,6 +888,24 @@ void Engine::homogenize_fe_batch(const std::vector<int> &gp_ids) {
     if (g.coupling == MICROPP3_FE_FULL && g.allocated) pert.push_back(i);
   }
 
+  // ctan by implicit differentiation at the converged state (u_k, vars_n): one 6-RHS tangent solve.
+  if (!pert.empty() && ctan_mode_ == MICROPP3_CTAN_IMPLICIT) {
+    for (int i : pert) {
+      GpState &g = gps_[gp_ids[i]];
+      h_insts_[i].vars_old = g.vars_n;
+    }
+    std::vector<int> its = tangent_solve(pert);
+    for (size_t a = 0; a < pert.size(); ++a) {
+      const int i = pert[a];
+      GpState &g = gps_[gp_ids[i]];
+      const InstOut &o = h_out_[i];
+      std::memcpy(g.ctan, o.ctan, sizeof(g.ctan));
+      g.cost += its[a];
+      if (o.nonfinite) g.status |= MICROPP3_STATUS_NONFINITE;
+    }
+    pert.clear();
+  }
+
   // ctan by 6 perturbed nonlinear solves (homogenize.cpp:256-275): u carried from u_k across the six
   // solves, history vars_n, cost charged with the main solve's CG count each time.
   if (!pert.empty()) {
@@ -752,8 +964,7 @@ void Engine::homogenize() {
     // Slots for as many points as memory allows (at most all of them).
     size_t free_b = 0, total_b = 0;
     check(cudaMemGetInfo(&free_b, &total_b), "mem info");
-    const double slot_bytes = 8.0 * (kEllPerNode * (double)mesh_.np + 8.0 * nndim() + 24.0 * mesh_.nelem + nvars());
-    const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes) + (int)slots_.size());
+    const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes()) + (int)slots_.size());
     const int want = std::min((int)fe.size(), fit);
     ensure_slots(want);
     const int per = (int)slots_.size();
@@ -803,9 +1014,18 @@ void Engine::get_newton(int gp, int *its, int *sits, int *conv) const {
 void Engine::calc_ctan_lin() {
   size_t free_b = 0, total_b = 0;
   check(cudaMemGetInfo(&free_b, &total_b), "mem info");
-  const double slot_bytes = 8.0 * (kEllPerNode * (double)mesh_.np + 8.0 * nndim() + 24.0 * mesh_.nelem + nvars());
-  const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes));
+  const int fit = std::max(1, (int)((double)free_b * 0.6 / slot_bytes()));
   ensure_slots(std::min(6, fit));
+  if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) {
+    // The linear ctan is the implicit derivative at u = 0 with no history: one 6-RHS tangent solve.
+    check(cudaMemsetAsync(slots_[0].u, 0, nndim() * sizeof(double), stream_), "u zero");
+    check(cudaMemsetAsync(slots_[0].out, 0, sizeof(InstOut), stream_), "out reset");
+    h_insts_[0].vars_old = nullptr;
+    h_insts_[0].has_vars_old = 0;
+    tangent_solve(std::vector<int>{0});
+    std::memcpy(ctan_lin_, h_out_[0].ctan, sizeof(ctan_lin_));
+    return;
+  }
   const int per = (int)slots_.size();
   for (int c0 = 0; c0 < 6; c0 += per) {
     const int cnt = std::min(per, 6 - c0);
@@ -943,10 +1163,114 @@ void Engine::print_info() const {
   std::cout << std::endl;
 }
 
+// output / write_vtu (output.cpp:29-214): element fields computed on the device (calc_fields,
+// average.cpp:84-112) from u_k and vars_n, written as the reference's ASCII VTU (<filename>.vtu).
 void Engine::output_vtu(int gp, const char *filename) {
-  (void)gp;
-  (void)filename;
-  throw std::runtime_error("VTU output is not available in this build");
+  const GpState &g = gps_.at(gp);
+  if (!g.u_k) throw std::runtime_error("output needs an FE-coupled Gauss point (it has no displacement field)");
+  const MeshDev &m = mesh_;
+  const double ivol = 1.0 / (m.wg * kNpe);
+  double *d_fields = dalloc<double>((size_t)12 * m.nelem, "fields");
+  std::vector<double> fields((size_t)12 * m.nelem), u(nndim()), vars;
+  try {
+    launches_ += 1;
+    check_launch(mgb_launch_elem_fields(&mesh_, &mats_, d_etype_, d_dsh_, g.u_k, g.allocated ? g.vars_n : nullptr,
+                                        ivol, d_fields, stream_),
+                 "element fields");
+    check(cudaMemcpyAsync(fields.data(), d_fields, fields.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+          "fields download");
+    sync();
+  } catch (...) {
+    dfree(d_fields);
+    throw;
+  }
+  dfree(d_fields);
+  get_u(gp, 1, u.data());
+  if (g.allocated) {
+    vars.resize(nvars());
+    get_vars(gp, 0, vars.data());
+  }
+  std::ofstream f(std::string(filename) + ".vtu");
+  if (!f) throw std::runtime_error("cannot open the VTU file for writing");
+  f << "<?xml version=\"1.0\"?>\n"
+    << "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
+    << "<UnstructuredGrid>\n"
+    << "<Piece NumberOfPoints=\"" << m.nn << "\" NumberOfCells=\"" << m.nelem << "\">\n"
+    << "<Points>\n"
+    << "<DataArray type=\"Float64\" Name=\"Position\" NumberOfComponents=\"3\" format=\"ascii\">" << std::endl;
+  f << std::scientific;
+  for (int k = 0; k < m.nz; ++k)
+    for (int j = 0; j < m.ny; ++j)
+      for (int i = 0; i < m.nx; ++i) f << i * m.dx << " " << j * m.dy << " " << k * m.dz << " \n";
+  f << "</DataArray>\n</Points>\n<Cells>\n" << std::endl;
+  f << "<DataArray type=\"Int32\" Name=\"connectivity\" NumberOfComponents=\"1\" format=\"ascii\">" << std::endl;
+  for (int ez = 0; ez < m.nez; ++ez)
+    for (int ey = 0; ey < m.ney; ++ey)
+      for (int ex = 0; ex < m.nex; ++ex) {
+        const int n0 = ez * m.nxny + ey * m.nx + ex;
+        for (int a = 0; a < 8; ++a) f << n0 + kCorner[a][2] * m.nxny + kCorner[a][1] * m.nx + kCorner[a][0] << ' ';
+        f << "\n";
+      }
+  f << "</DataArray>" << std::endl;
+  f << "<DataArray type=\"Int32\" Name=\"offsets\" NumberOfComponents=\"1\" format=\"ascii\">" << std::endl;
+  for (int e = 0, ce = 8; e < m.nelem; ++e, ce += 8) f << ce << " ";
+  f << "\n</DataArray>" << std::endl;
+  f << "<DataArray type=\"UInt8\"  Name=\"types\" NumberOfComponents=\"1\" format=\"ascii\">" << std::endl;
+  for (int e = 0; e < m.nelem; ++e) f << 12 << " ";
+  f << "\n</DataArray>" << std::endl;
+  f << "</Cells>" << std::endl;
+  f << "<PointData Vectors=\"displ\" >" << std::endl;
+  f << "<DataArray type=\"Float64\" Name=\"displ\" NumberOfComponents=\"3\" format=\"ascii\" >" << std::endl;
+  for (int n = 0; n < m.nn; ++n) {
+    for (int d = 0; d < 3; ++d) f << u[n * 3 + d] << " ";
+    f << "\n";
+  }
+  f << "</DataArray>" << std::endl;
+  f << "</PointData>" << std::endl;
+  f << "<CellData>" << std::endl;
+  f << "<DataArray type=\"Float64\" Name=\"strain\" NumberOfComponents=\"6\" format=\"ascii\">" << std::endl;
+  for (int e = 0; e < m.nelem; ++e) {
+    for (int v = 0; v < 6; ++v) f << fields[(size_t)e * 12 + v] << " ";
+    f << "\n";
+  }
+  f << "</DataArray>\n";
+  f << "<DataArray type=\"Float64\" Name=\"stress\" NumberOfComponents=\"6\" format=\"ascii\">" << std::endl;
+  for (int e = 0; e < m.nelem; ++e) {
+    for (int v = 0; v < 6; ++v) f << fields[(size_t)e * 12 + 6 + v] << " ";
+    f << "\n";
+  }
+  f << "</DataArray>\n";
+  f << "<DataArray type=\"Int32\" Name=\"elem_type\" NumberOfComponents=\"1\" format=\"ascii\">" << std::endl;
+  for (int e = 0; e < m.nelem; ++e) f << (int)etype_[e] << " ";
+  f << "\n</DataArray>" << std::endl;
+  // Per element: the plastic-strain norm field keeps the reference's expression (x + sqrt(x), output.cpp:162-175),
+  // then the averages of r (damage_e), D (damage_D) and alpha (hardening) over the 8 Gauss points.
+  auto var = [&](int e, int gpi, int v) { return vars.empty() ? 0.0 : vars[((size_t)e * 8 + gpi) * kNvarGp + v]; };
+  f << "<DataArray type=\"Float64\" Name=\"plasticity\" NumberOfComponents=\"1\" format=\"ascii\">" << std::endl;
+  for (int e = 0; e < m.nelem; ++e) {
+    double pl = 0.0;
+    for (int gpi = 0; gpi < 8; ++gpi)
+      for (int v = 0; v < 6; ++v) pl += var(e, gpi, v) * var(e, gpi, v);
+    pl += std::sqrt(pl);
+    f << pl / 8 << " ";
+  }
+  f << "\n</DataArray>" << std::endl;
+  const char *names[3] = {"damage_e", "damage_D", "hardening"};
+  const int idx[3] = {0, 1, 6};
+  for (int q = 0; q < 3; ++q) {
+    f << "<DataArray type=\"Float64\" Name=\"" << names[q] << "\" NumberOfComponents=\"1\" format=\"ascii\">"
+      << std::endl;
+    for (int e = 0; e < m.nelem; ++e) {
+      double a = 0.0;
+      for (int gpi = 0; gpi < 8; ++gpi) a += var(e, gpi, idx[q]);
+      f << a / 8 << " ";
+    }
+    f << "\n</DataArray>" << std::endl;
+  }
+  f << "</CellData>" << std::endl;
+  f << "</Piece>" << std::endl;
+  f << "</UnstructuredGrid>" << std::endl;
+  f << "</VTKFile>" << std::endl;
 }
 
 }  // namespace mgb

@@ -39,8 +39,13 @@ struct GpState {
 struct Slot {
   double *u = nullptr, *du = nullptr, *b = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr;
   double *kinv = nullptr, *vals = nullptr, *be = nullptr, *vars_aux = nullptr, *red = nullptr;
+  float *vals32 = nullptr, *kinv32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr,
+        *du32 = nullptr;
+  double *X6 = nullptr, *F6 = nullptr;
+  float *R6 = nullptr, *Z6 = nullptr, *P6 = nullptr, *AP6 = nullptr, *D6 = nullptr;
   unsigned int *ticket = nullptr;
   CgState *cg = nullptr;
+  Cg6State *cg6 = nullptr;
   InstOut *out = nullptr;
 };
 
@@ -118,6 +123,9 @@ class Engine {
   void download_out();
   void residual(const std::vector<int> &slots);
   void cg_solve(const std::vector<int> &slots);
+  void cg_solve32(const std::vector<int> &slots);
+  std::vector<int> tangent_solve(const std::vector<int> &slots);
+  double slot_bytes() const;
   std::vector<NewtonResult> newton(const std::vector<int> &slots, const std::vector<std::array<double, 6>> &strains);
   void homogenize_fe_batch(const std::vector<int> &gp_ids);
   void allocate_vars(GpState &g);
@@ -150,6 +158,7 @@ class Engine {
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
+  float *d_ke32_ = nullptr;
   std::vector<Slot> slots_;
   std::vector<Inst> h_insts_;
   Inst *d_insts_ = nullptr;
@@ -160,7 +169,7 @@ class Engine {
   double last_ms_ = 0.0;
   long total_cg_its_ = 0;
   long launches_ = 0;  // kernels of this library launched by the handle
-  KernelTimer t_spmv_, t_update_, t_asm_, t_res_;
+  KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_;
 };
 
 }  // namespace mgb

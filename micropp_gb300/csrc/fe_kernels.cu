@@ -211,13 +211,27 @@ constexpr int kMatElems = 8;
 
 __device__ __forceinline__ int ell_idx(int s, int fi, int fj) { return s * 9 + fi * 3 + fj; }
 
+template <typename T>
+__device__ __forceinline__ T *ell_values(const Inst &I);
+template <>
+__device__ __forceinline__ double *ell_values<double>(const Inst &I) {
+  return I.vals;
+}
+template <>
+__device__ __forceinline__ float *ell_values<float>(const Inst &I) {
+  return I.vals32;
+}
+
+// T = double: the plain FP64 Jacobian.  T = float: the mixed form's FP32 Jacobian -- the Gauss-point tangents
+// are still formed in FP64 (forward differences need it) and rounded once; Ke is accumulated in FP32.
+template <typename T>
 __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mats, const int8_t *etype,
-                                                              const double *dsh_g, const double *ke_phase,
+                                                              const double *dsh_g, const T *ke_phase,
                                                               const Inst *insts, const int *list, int color) {
   __shared__ double dsh[8 * 24];
   __shared__ double ue[kMatElems][24];
-  __shared__ double Cg[kMatElems][8][36];
-  __shared__ double cxb[kMatElems][6 * 24];
+  __shared__ T Cg[kMatElems][8][36];
+  __shared__ T cxb[kMatElems][6 * 24];
   for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
   const Inst &I = insts[list[blockIdx.y]];
   const int cx = color & 1, cy = (color >> 1) & 1, cz = (color >> 2) & 1;
@@ -241,43 +255,46 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
   }
   __syncthreads();
   const bool nonlin = valid && law != 0;
-  // Gauss-point tangents.
+  // Gauss-point tangents (FP64).
   if (nonlin && p < 8) {
-    double eps[6];
+    double eps[6], C[36];
     gp_strain(&dsh[p * 24], ue[el], eps);
-    law_ctan(mats.m[ph], eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr, Cg[el][p]);
+    law_ctan(mats.m[ph], eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr, C);
+#pragma unroll
+    for (int i = 0; i < 36; ++i) Cg[el][p][i] = (T)C[i];
   }
   __syncthreads();
-  double row[24];
+  T row[24];
   const int a = p / 3, d = p % 3;
   // Non-zero rows m of column p of B in ascending order, and their coefficients.
   const int m0 = d, m1 = (d == 0) ? 3 : (d == 1 ? 3 : 4), m2 = (d == 0) ? 4 : 5;
   if (nonlin) {
 #pragma unroll
-    for (int q = 0; q < 24; ++q) row[q] = 0.0;
+    for (int q = 0; q < 24; ++q) row[q] = (T)0;
   } else if (valid) {
-    const double *K = ke_phase + (size_t)ph * 576 + p * 24;
+    const T *K = ke_phase + (size_t)ph * 576 + p * 24;
 #pragma unroll
     for (int q = 0; q < 24; ++q) row[q] = K[q];
   }
+  const T wg = (T)m.wg;
 #pragma unroll 1
   for (int g = 0; g < 8; ++g) {
     const double *dg = &dsh[g * 24];
     // B column p has B[m0][p], B[m1][p], B[m2][p] non-zero.
-    const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
-    const double bp0 = (d == 0) ? gx : (d == 1 ? gy : gz);
-    const double bp1 = (d == 0) ? gy : gx;
-    const double bp2 = (d == 0) ? gz : (d == 1 ? gz : gy);
+    const T gx = (T)dg[a * 3], gy = (T)dg[a * 3 + 1], gz = (T)dg[a * 3 + 2];
+    const T bp0 = (d == 0) ? gx : (d == 1 ? gy : gz);
+    const T bp1 = (d == 0) ? gy : gx;
+    const T bp2 = (d == 0) ? gz : (d == 1 ? gz : gy);
     if (nonlin) {
       // cxb[mm][p] = wg * sum_k C[mm][k] B[k][p] over the non-zero k of column p (ascending).
-      const double *C = Cg[el][g];
+      const T *C = Cg[el][g];
 #pragma unroll
       for (int mm = 0; mm < 6; ++mm) {
-        double t = 0.0;
+        T t = (T)0;
         t += C[mm * 6 + m0] * bp0;
         t += C[mm * 6 + m1] * bp1;
         t += C[mm * 6 + m2] * bp2;
-        cxb[el][mm * 24 + p] = t * m.wg;
+        cxb[el][mm * 24 + p] = t * wg;
       }
     }
     __syncthreads();
@@ -297,22 +314,24 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
   const int gi = ex + ai, gj = ey + aj, gk = ez + ak;
   if (is_boundary(m, gi, gj, gk)) return;
   const int node = n0 + ak * m.nxny + aj * m.nx + ai;
+  T *vals = ell_values<T>(I);
 #pragma unroll
   for (int b = 0; b < 8; ++b) {
     const int s = (c_corner[b][2] - ak + 1) * 9 + (c_corner[b][1] - aj + 1) * 3 + (c_corner[b][0] - ai + 1);
 #pragma unroll
     for (int fj = 0; fj < 3; ++fj) {
-      double *dst = &I.vals[(size_t)ell_idx(s, d, fj) * m.np + node];
+      T *dst = &vals[(size_t)ell_idx(s, d, fj) * m.np + node];
       *dst += row[b * 3 + fj];
     }
   }
 }
 
 // Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
+template <typename T>
 __global__ void k_zero_vals(size_t count, const Inst *insts, const int *list) {
-  double *v = insts[list[blockIdx.y]].vals;
+  T *v = ell_values<T>(insts[list[blockIdx.y]]);
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
-    v[t] = 0.0;
+    v[t] = (T)0;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -348,6 +367,46 @@ __global__ void __launch_bounds__(kNodeBlock) k_evolve(MeshDev m, Mats mats, con
   if (__syncthreads_or(nl) && threadIdx.x == 0) atomicOr(&I.out->nonlinear, 1);
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Element averages of strain and stress for field output, calc_fields (average.cpp:84-112):
+// fields[e*12 + v] = sum_gp strain_v wg * ivol, fields[e*12 + 6 + v] = sum_gp stress_v wg * ivol.
+__global__ void __launch_bounds__(kElemBlock) k_elem_fields(MeshDev m, Mats mats, const int8_t *etype,
+                                                              const double *dsh_g, const double *u,
+                                                              const double *vars, double ivol, double *fields) {
+  __shared__ double dsh[8 * 24];
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelem) return;
+  const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
+  const int n0 = ez * m.nxny + ey * m.nx + ex;
+  double ue[24];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) ue[a * 3 + d] = u[n * 3 + d];
+  }
+  const MatDev &mat = mats.m[etype[e]];
+  double ea[6] = {0, 0, 0, 0, 0, 0}, sa[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+  for (int g = 0; g < 8; ++g) {
+    double eps[6], s[6];
+    gp_strain(&dsh[g * 24], ue, eps);
+    law_stress(mat, eps, vars ? vars + ((size_t)e * 8 + g) * kNvarGp : nullptr, s);
+#pragma unroll
+    for (int v = 0; v < 6; ++v) {
+      ea[v] += eps[v] * m.wg;
+      sa[v] += s[v] * m.wg;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 6; ++v) {
+    fields[(size_t)e * 12 + v] = ea[v] * ivol;
+    fields[(size_t)e * 12 + 6 + v] = sa[v] * ivol;
+  }
+}
+
 }  // namespace mgb
 
 // ---------------------------------------------------------------------------------------------------
@@ -356,6 +415,22 @@ __global__ void __launch_bounds__(kNodeBlock) k_evolve(MeshDev m, Mats mats, con
 using namespace mgb;
 
 static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+template <typename T>
+static int launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh, const T *ke_phase,
+                           const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const size_t count = (size_t)kEllPerNode * m->np;
+  k_zero_vals<T><<<dim3(cdiv(count, 8 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(count, insts, list);
+  for (int c = 0; c < 8; ++c) {
+    const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
+    const int nce = ((m->nex - cx + 1) / 2) * ((m->ney - cy + 1) / 2) * ((m->nez - cz + 1) / 2);
+    if (nce <= 0) continue;
+    k_elem_mat<T><<<dim3(cdiv(nce, kMatElems), nlist), kMatElems * 24, 0, s>>>(*m, *mats, etype, dsh, ke_phase,
+                                                                               insts, list, c);
+  }
+  return (int)cudaGetLastError();
+}
 
 extern "C" {
 
@@ -388,16 +463,17 @@ int mgb_launch_residual(const MeshDev *m, const Mats *mats, const int8_t *etype,
 
 int mgb_launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
                         const double *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
-  if (nlist <= 0) return 0;
-  const size_t count = (size_t)kEllPerNode * m->np;
-  k_zero_vals<<<dim3(cdiv(count, 8 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(count, insts, list);
-  for (int c = 0; c < 8; ++c) {
-    const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
-    const int nce = ((m->nex - cx + 1) / 2) * ((m->ney - cy + 1) / 2) * ((m->nez - cz + 1) / 2);
-    if (nce <= 0) continue;
-    k_elem_mat<<<dim3(cdiv(nce, kMatElems), nlist), kMatElems * 24, 0, s>>>(*m, *mats, etype, dsh, ke_phase,
-                                                                            insts, list, c);
-  }
+  return launch_assembly<double>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
+}
+
+int mgb_launch_assembly32(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
+                          const float *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  return launch_assembly<float>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
+}
+
+int mgb_launch_elem_fields(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh, const double *u,
+                           const double *vars, double ivol, double *fields, cudaStream_t s) {
+  k_elem_fields<<<cdiv(m->nelem, kElemBlock), kElemBlock, 0, s>>>(*m, *mats, etype, dsh, u, vars, ivol, fields);
   return (int)cudaGetLastError();
 }
 

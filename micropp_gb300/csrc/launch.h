@@ -24,11 +24,32 @@ int mgb_launch_assembly(const mgb::MeshDev *m, const mgb::Mats *mats, const int8
                         const double *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_evolve(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                       const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_elem_fields(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                           const double *u, const double *vars, double ivol, double *fields, cudaStream_t s);
 int mgb_launch_cg_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                           unsigned int *active_count, cudaStream_t s);
+
+int mgb_launch_assembly32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                          const float *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg32_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
+                            unsigned int *active_count, cudaStream_t s);
+int mgb_launch_add_du32(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg6_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg6_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
+                           unsigned int *active_count, cudaStream_t s);
+int mgb_launch_t6_accumulate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
+                             cudaStream_t s);
+int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                        const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -263,6 +263,7 @@ class RefRVE(_Base):
             self._setup()
             lib.ref_write_restart.argtypes = [C.c_void_p, C.c_int]
             lib.ref_read_restart.argtypes = [C.c_void_p, C.c_int]
+            lib.ref_output.argtypes = [C.c_void_p, C.c_int, C.c_char_p]
         self.lib = RefRVE.libs[variant]
         super().__init__(cfg)
 
@@ -271,6 +272,9 @@ class RefRVE(_Base):
 
     def read_restart(self, restart_id):
         self.lib.ref_read_restart(self.h, restart_id)
+
+    def output(self, gp, filename):
+        self.lib.ref_output(self.h, gp, filename.encode())
 
 
 def ref_available(variant="stock"):

@@ -105,4 +105,5 @@ void ref_get_vars(void *h, int gp, int which, double *out) { ((ref_rve *)h)->var
 void ref_get_u(void *h, int gp, int which, double *out) { ((ref_rve *)h)->u(gp, which, out); }
 void ref_write_restart(void *h, int id) { ((ref_rve *)h)->write_restart(id); }
 void ref_read_restart(void *h, int id) { ((ref_rve *)h)->read_restart(id); }
+void ref_output(void *h, int gp, const char *filename) { ((ref_rve *)h)->output(gp, filename); }
 }

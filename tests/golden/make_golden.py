@@ -6,6 +6,8 @@
 2. ref_<case>.npz -- outputs of the compiled reference on the seeded parity cases of tests/cases.py:
    per step and Gauss point the average stress, ctan, cost, flags, and the internal variables and the
    displacement of the last step.
+3. ref_output_damage.vtu -- the reference's VTU field output (micropp<3>::output) of a 3^3 damage RVE after
+   one nonlinear step, and ref_output_j2.vtu for a J2 matrix.
 
 Usage: python tests/golden/make_golden.py [reference_root]   (needs oracle/build_ref.sh to have run)
 """
@@ -82,6 +84,16 @@ def run_case(name):
     np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **arrays)
 
 
+def vtu_cases():
+    """(tag, config keywords, strain path) of the VTU fixtures (shared with tests/test_gpu_output.py)."""
+    import numpy as np
+    dmg = [orc.material(2, 1e7, 0.25, 0, 0, 1e5), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    j2 = [orc.material(1, 1e7, 0.3, 1e5, 1e4), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    common = dict(micro_type=1, geo=(0.3, 0, 0, 0), coupling=[2], lin_stress=0, nr_max_its=12, nr_max_tol=1e-5)
+    return [("damage", dict(mats=dmg, **common), [np.array([3e-2, -1e-2, 0, 1e-2, 0, 0])]),
+            ("j2", dict(mats=j2, **common), [np.array([1e-2, 0, 0, 2e-3, 0, 0]) * s for s in (1, 2)])]
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tables = {}
@@ -93,6 +105,16 @@ def main():
         json.dump(tables, f, indent=1)
     for name in ("c1_sphere_elastic", "damage_layers", "plastic_sphere"):
         run_case(name)
+    for tag, cfg_kw, eps in vtu_cases():
+        r = orc.RefRVE(orc.make_config(3, **cfg_kw))
+        for e in eps:
+            r.set_strain(0, e)
+            r.homogenize()
+            r.update_vars()
+        r.set_strain(0, eps[-1] * 1.2)
+        r.homogenize()
+        r.output(0, os.path.join(HERE, f"ref_output_{tag}"))
+        r.close()
     print("wrote fixtures to", HERE)
 
 
