@@ -123,6 +123,19 @@ int micropp3_kernel_stats(const struct micropp3 *self, const char *family, long 
 int micropp3_ell_solve_cgpd(const int nodes[3], const double *vals, const double *b, double *x, double rel_tol,
                             double abs_tol, int max_its, int *its, void *stream);
 
+/* The same solve as micropp3_ell_solve_cgpd, for callers that must not allocate device memory while they
+ * run (a code that has already handed the device to its own memory pool, or a time step that must not wait
+ * on the allocator).  This entry point has no counterpart in the reference.  Its work vectors live in one
+ * fixed array of device memory that the library holds on every GPU where it is loaded, until the process
+ * exits (about 16 MB), so the grid may have at most MICROPP3_NOALLOC_MAX_NODES nodes (50 x 50 x 50);
+ * larger grids return -3.  The caller passes vals, b and x as for micropp3_ell_solve_cgpd.  The first call on
+ * a device resolves the array's address on that device; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU (other host threads, other streams) race and must be serialised.
+ * Returns 0, -1 for invalid arguments, -3 for a grid over the limit, or the CUDA error code. */
+#define MICROPP3_NOALLOC_MAX_NODES 131072
+int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, const double *b, double *x,
+                                    double rel_tol, double abs_tol, int max_its, int *its, void *stream);
+
 /* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
 long micropp3_total_cg_its(const struct micropp3 *self);
 long micropp3_kernel_launches(const struct micropp3 *self);

@@ -112,6 +112,8 @@ def load():
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
         "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                              C.c_int, ip, C.c_void_p]),
+        "micropp3_ell_solve_cgpd_noalloc": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                                     C.c_double, C.c_int, ip, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

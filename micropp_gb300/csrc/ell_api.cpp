@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "ell_api.h"
 #include "launch.h"
 #include "micropp_gb300.h"
 
