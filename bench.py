@@ -1,17 +1,20 @@
 #!/usr/bin/env python
-"""RVE homogenizations/s (stress + ctan) at 60^3 on one GB300.
+"""RVE homogenizations/s (stress + ctan) at 60^3 on one GB300: the fast form against the plain form.
 
 Workload (default): R = 32 damage RVEs of 60^3 elements (226,981 nodes, 680,943 DOF each): 4 stiff layers
-normal to z (E = 1e8, nu = 0.25, 0.1 thick), damage matrix (E = 1e7, nu = 0.25, Xt = 1e5), FE_FULL coupling with lin_stress off, Newton <= 12 iterations at tolerance 1e-5, DPCG at the
-reference's 1e-5.  Each RVE has a seeded macro strain target ~ U[-2.5e-2, 2.5e-2]^6 (scaled up until the
-RVE is nonlinear).  Set-up loads every RVE to half its target and accepts the step; a bench step is one
-macro iteration: every RVE is homogenized (stress and ctan: one Newton solve plus six perturbed solves) at
-its target strain, through the public C ABI.  Inputs are synthetic (no dataset is involved).
+normal to z (E = 1e8, nu = 0.25, 0.1 thick), damage matrix (E = 1e7, nu = 0.25, Xt = 1e5), FE_FULL coupling
+with lin_stress off.  Each RVE has a seeded macro strain target ~ U[-2.5e-2, 2.5e-2]^6.  Set-up loads every
+RVE to half its target and accepts the step; a bench step is one macro iteration: every RVE is homogenized
+(stress and ctan) at its target strain through the public C ABI.  Inputs are synthetic.
 
-One JSON line is printed by rank 0.  `value` is the device-timed throughput (CUDA events on the handles'
-streams); `e2e` is the wall-clock throughput of the same C-ABI calls with host strain/stress/ctan buffers.
-`--impl reference` times the reference's CPU algorithm (the oracle port of it, since the compiled reference
-cannot run on this host) on all host cores, on a bounded sample of the same workload.
+Two forms are measured on the same workload, one after the other (FORMS below):
+  fast  -- FP32 Jacobian and CG inside FP64 refinement, ctan by implicit differentiation (headline `value`);
+  plain -- the reference algorithm in FP64 (Newton + DPCG at the reference's tolerances, ctan from six
+           perturbed Newton solves), the drop-in form.
+`value` is device-timed throughput (CUDA events on the handles' streams); `e2e` the wall-clock throughput of
+the same C-ABI calls with host strain/stress/ctan buffers; `forms` holds both forms' figures and
+`fast_over_plain` their ratio.  `--impl reference` times the reference's CPU algorithm (the oracle port of
+it, since the compiled reference cannot run on this host) on all host cores, on a bounded sample.
 """
 import argparse
 import json
@@ -47,6 +50,7 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample-rves", type=int, default=0, help="RVEs in the CPU sample (default: host cores)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--forms", default="fast,plain", help="forms to measure; the first is the headline value")
     return p.parse_args()
 
 
@@ -66,11 +70,20 @@ def workload(n, rves, seed, rank):
     return wl.layers_z(n), xts, targets
 
 
-def gpu_config(n, et, xt):
+# The two forms.  plain: the reference algorithm in FP64 (Newton to the reference's tolerances, ctan from six
+# perturbed Newton solves).  fast: FP32 Jacobian and CG inside FP64 refinement, Newton converged to 1e-8 of the
+# initial residual (average stress within 1e-7 of the converged FP64 solution), ctan by implicit
+# differentiation (one 6-RHS tangent solve).
+FORMS = {
+    "plain": dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5),
+    "fast": dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8),
+}
+
+
+def gpu_config(n, et, xt, form="plain"):
     import micropp_gb300 as mg
     mats = [mg.material(2, 1e7, 0.25, 0, 0, xt), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
-    return mg.config(n, mats=mats, coupling=[2], elem_type=et, lin_stress=0, nr_max_its=12, nr_max_tol=1e-5,
-                     calc_ctan_lin=0)
+    return mg.config(n, mats=mats, coupling=[2], elem_type=et, lin_stress=0, calc_ctan_lin=0, **FORMS[form])
 
 
 # ---------------------------------------------------------------------------------------------------------
@@ -240,44 +253,35 @@ def run_reference(args):
     }))
 
 
-def load_traffic(n):
-    """DRAM bytes per SpMV launch from the committed ncu summary (profiles/), if present."""
-    p = os.path.join(ROOT, "profiles", "spmv_fp64_traffic.json")
-    if os.path.exists(p):
+def load_traffic(n, family="spmv", fp32=False):
+    """DRAM bytes per launch of the kernel from a committed ncu summary (profiles/*_traffic.json), if any."""
+    name = {("spmv", False): "spmv_fp64", ("spmv", True): "spmv_fp32", ("spmv6", True): "spmv6_fp32"}.get((family, fp32))
+    p = os.path.join(ROOT, "profiles", f"{name}_traffic.json") if name else ""
+    if name and os.path.exists(p):
         d = json.load(open(p))
         return d.get("bytes_per_launch_at_n", {}).get(str(n))
     return None
 
 
-def run_gpu(args):
-    world, rank, local, pg = dist_setup(args)
+def measure_form(args, form, et, xts, targets, L, pg, world, local):
+    """Set up R RVEs in `form`, run W warm-up and K timed steps; returns the figures of this form."""
     import ctypes
 
     import micropp_gb300 as mg
-    from micropp_gb300 import build
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
-    build.build()
-    L = mg.load()
-    if world > 1:
-        import torch
-        torch.cuda.set_device(local)
     n, R = args.size, args.rves
-    et, xts, targets = workload(n, R, args.seed, rank)
-    handles = []
-    for i in range(R):
-        handles.append(mg.Micropp(gpu_config(n, et, float(xts[i]))))
+    handles = [mg.Micropp(gpu_config(n, et, float(xts[i]), form)) for i in range(R)]
     # Set-up: load each RVE to half its target and accept the step; grow the target until it is nonlinear.
+    tg = [t.copy() for t in targets]
     for i, h in enumerate(handles):
         for _ in range(4):
-            h.set_strain(0, 0.5 * targets[i])
+            h.set_strain(0, 0.5 * tg[i])
             h.homogenize()
             if h.is_non_linear(0):
                 break
-            targets[i] *= 1.5
+            tg[i] *= 1.5
         h.update_vars()
     nonlinear = sum(h.is_non_linear(0) for h in handles)
-
-    strain_bufs = [np.ascontiguousarray(t, dtype=np.float64) for t in targets]
+    strain_bufs = [np.ascontiguousarray(t, dtype=np.float64) for t in tg]
     out_s = np.zeros((R, 6))
     out_c = np.zeros((R, 36))
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
@@ -311,61 +315,114 @@ def run_gpu(args):
     launches = sum(h.kernel_launches() for h in handles) - l0
     if L.micropp3_last_error():
         raise RuntimeError(L.micropp3_last_error().decode())
-    assert np.isfinite(out_s).all() and np.isfinite(out_c).all()
+    status = [h.status(0) for h in handles]
+    finite = bool(np.isfinite(out_s).all() and np.isfinite(out_c).all())
     stats = {}
-    for fam in ("spmv", "cg_update", "assembly", "residual"):
+    for fam in ("spmv", "spmv6", "cg_update", "assembly", "residual"):
         tot = [h.kernel_stats(fam) for h in handles]
         stats[fam] = (sum(t[0] for t in tot), sum(t[1] for t in tot), sum(t[2] for t in tot))
+    for h in handles:
+        h.close()
     dev_s = max_over_ranks(pg, dev_ms / 1e3, world)
     wall_s = max_over_ranks(pg, wall, world)
     homs = R * args.steps * world
-    value = homs / dev_s
-    e2e = homs / wall_s
+    return {"form": form, "value": homs / dev_s, "e2e": homs / wall_s, "dev_s": dev_s, "wall_s": wall_s,
+            "cg_its": cg_its, "launches": launches, "stats": stats, "clocks": clk.summary(),
+            "nonlinear": nonlinear, "status": status, "finite": finite, "stress": out_s.copy(), "ctan": out_c.copy()}
+
+
+def roofline_of(res, n, peak, peak_kind):
+    """Roofline record of the form's dominant linear-algebra kernel (most device time)."""
+    nrow = 3 * (n + 1) ** 3
+    fp32 = res["form"] == "fast"
+    cands = {"spmv": res["stats"]["spmv"], "spmv6": res["stats"]["spmv6"]}
+    fam = max(cands, key=lambda k: cands[k][1])
+    nk, ms, by = cands[fam]
+    achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
+    if fam == "spmv6":
+        name, per = "k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides)", nrow * (81 * 4 + 12 * 4)
+    elif fp32:
+        name, per = "k_cg32_spmv (FP32 ELL SpMV + p.Ap)", nrow * (81 * 4 + 2 * 4)
+    else:
+        name, per = "k_cg_spmv (FP64 ELL SpMV + p.Ap)", nrow * (81 * 8 + 2 * 8)
+    traffic = load_traffic(n, fam, fp32)
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": per, "launches": nk, "avg_us": 1e3 * ms / nk if nk else None}
+
+
+def run_gpu(args):
+    world, rank, local, pg = dist_setup(args)
+    import micropp_gb300 as mg
+    from micropp_gb300 import build
+    build.build()
+    L = mg.load()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+    n, R = args.size, args.rves
+    et, xts, targets = workload(n, R, args.seed, rank)
+    forms = [f for f in args.forms.split(",") if f]
+    results = [measure_form(args, f, et, xts, targets, L, pg, world, local) for f in forms]
     if rank != 0:
         return
+    head = results[0]
     peaks = {}
     pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pp):
         peaks = json.load(open(pp))
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
-    nk, ms, by = stats["spmv"]
-    achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
-    traffic = load_traffic(n)
     nrow = 3 * (n + 1) ** 3
-    per_launch_bytes = nrow * (81 * 8 + 2 * 8)
     cpu = None
     if not args.no_cpu_baseline:
         cores = args.cpu_sample_rves or host_cores()
-        dt, its = cpu_sample(n, xts, targets, cores)
-        per_hom = cg_its / (R * args.steps)
-        cpu_val = its / per_hom / dt
-        cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": (f"one Newton iteration (residual, assembly, DPCG of {its // cores} its avg, residual) of "
-                          f"{cores} RVEs of the workload at half strain, OpenMP over RVEs, {dt:.1f} s; scaled by "
-                          f"{per_hom:.0f} CG its per stress+ctan homogenization measured in this run")}
+        plain = next((r for r in results if r["form"] == "plain"), None)
+        ref_its = (plain["cg_its"] / (R * args.steps)) if plain else CG_ITS_PER_HOM.get(n)
+        if ref_its:
+            dt, its = cpu_sample(n, xts, targets, cores)
+            cpu_val = its / ref_its / dt
+            cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": (f"one Newton iteration (residual, assembly, DPCG of {its // cores} its avg, residual) of "
+                              f"{cores} RVEs of the workload at half strain, OpenMP over RVEs, {dt:.1f} s; scaled by "
+                              f"{ref_its:.0f} CG its per stress+ctan homogenization of the reference algorithm "
+                              f"(the plain form, measured in this run)")}
+
+    def form_record(r):
+        return {"value": r["value"], "e2e": r["e2e"], "ms_per_step": 1e3 * r["dev_s"] / args.steps,
+                "cg_its_per_homogenization": r["cg_its"] / (R * args.steps),
+                "cg_its_per_s": r["cg_its"] * world / r["dev_s"],
+                "dof_updates_per_s": r["cg_its"] * nrow * world / r["dev_s"],
+                "nonlinear_rves": r["nonlinear"], "finite": r["finite"],
+                "status_counts": {str(k): r["status"].count(k) for k in sorted(set(r["status"]))},
+                "gpu_launches": r["launches"], "roofline": roofline_of(r, n, peak, peak_kind),
+                "kernels": {k: {"launches": v[0], "ms": v[1], "avg_us": 1e3 * v[1] / v[0] if v[0] else None,
+                                "algorithmic_GBps": v[2] / (v[1] / 1e3) / 1e9 if v[1] else None}
+                            for k, v in r["stats"].items() if v[0]}}
+
+    extra = {r["form"]: form_record(r) for r in results}
+    ratio = None
+    if len(results) > 1:
+        ratio = results[0]["value"] / results[1]["value"]
+        s0, s1 = results[0]["stress"], results[1]["stress"]
+        extra["stress_rel_diff_between_forms"] = float(np.max(np.abs(s0 - s1)) / np.max(np.abs(s1)))
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * head["dev_s"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if head["form"] == "fast" else "f64",
+        "data": "synthetic",
         "config": {"workload": f"{R} damage RVEs of {n}^3 per GPU (4 layers normal to z, Xt=1e5), "
-                               f"FE_FULL stress+ctan (1 + 6 perturbed Newton solves), plain FP64 form",
-                   "n": n, "rves_per_gpu": R, "form": "plain-fp64", "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (441 MB ELL per RVE)", "nonlinear_rves": nonlinear},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 6 * 8, "d2h_bytes_per_step": R * 42 * 8},
-        "roofline": {"bound": "hbm", "kernel": "k_cg_spmv (FP64 ELL SpMV + p.Ap)", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
-                     "launches": nk, "avg_us": 1e3 * ms / nk if nk else None},
+                               f"FE_FULL stress+ctan, one homogenization per RVE per step",
+                   "n": n, "rves_per_gpu": R, "form": head["form"], "forms_measured": forms,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (221-441 MB ELL per RVE)"},
+        "e2e": {"value": head["e2e"], "unit": UNIT, "h2d_bytes_per_step": R * 6 * 8, "d2h_bytes_per_step": R * 42 * 8},
+        "roofline": roofline_of(head, n, peak, peak_kind),
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
-        "gpu_launches": launches,
-        "cg_its_per_s": cg_its * world / dev_s,
-        "dof_updates_per_s": cg_its * nrow * world / dev_s,
-        "cg_its_per_homogenization": cg_its / (R * args.steps),
-        "kernels": {k: {"launches": v[0], "ms": v[1], "avg_us": 1e3 * v[1] / v[0] if v[0] else None,
-                        "algorithmic_GBps": v[2] / (v[1] / 1e3) / 1e9 if v[1] else None}
-                    for k, v in stats.items()},
+        "clocks": head["clocks"],
+        "gpu_launches": head["launches"],
+        "fast_over_plain": ratio,
+        "forms": extra,
     }
     print(json.dumps(line))
 

@@ -34,17 +34,24 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_setup(MeshDev m, const Inst *
   if (n < m.nn) {
     int i, j, k;
     const bool bnd = node_boundary(m, n, i, j, k);
+    const double *__restrict__ vals = I.vals;
+    const double *__restrict__ b = I.b;
+    double *__restrict__ kinv = I.kinv;
+    double *__restrict__ x = I.du;
+    double *__restrict__ rv = I.r;
+    double *__restrict__ zv = I.z;
+    double *__restrict__ pv = I.p;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int row = n * 3 + d;
-      const double kd = bnd ? 1.0 : 1 / I.vals[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
-      const double r = I.b[row];
+      const double kd = bnd ? 1.0 : 1 / vals[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+      const double r = b[row];
       const double z = kd * r;
-      I.kinv[row] = kd;
-      I.du[row] = 0.0;
-      I.r[row] = r;
-      I.z[row] = z;
-      I.p[row] = z;
+      kinv[row] = kd;
+      x[row] = 0.0;
+      rv[row] = r;
+      zv[row] = z;
+      pv[row] = z;
       acc[0] += r * z;
       acc[1] += z * z;
     }
@@ -74,11 +81,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_spmv(MeshDev m, const Inst *i
   if (n < m.nn) {
     int i, j, k;
     const double *__restrict__ p = I.p;
+    double *__restrict__ Ap = I.Ap;
     if (node_boundary(m, n, i, j, k)) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const double pv = p[n * 3 + d];
-        I.Ap[n * 3 + d] = pv;
+        Ap[n * 3 + d] = pv;
         acc[0] += pv * pv;
       }
     } else {
@@ -100,9 +108,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_spmv(MeshDev m, const Inst *i
         y2 += __ldcs(vs + 7 * np) * x1;
         y2 += __ldcs(vs + 8 * np) * x2;
       }
-      I.Ap[n * 3 + 0] = y0;
-      I.Ap[n * 3 + 1] = y1;
-      I.Ap[n * 3 + 2] = y2;
+      Ap[n * 3 + 0] = y0;
+      Ap[n * 3 + 1] = y1;
+      Ap[n * 3 + 2] = y2;
       acc[0] = p[n * 3 + 0] * y0 + p[n * 3 + 1] * y1 + p[n * 3 + 2] * y2;
     }
   }
@@ -121,13 +129,19 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_update(MeshDev m, const Inst 
   if (cs->done) return;
   const double alpha = cs->alpha;
   const int nrow = m.nn * 3;
+  double *__restrict__ x = I.du;
+  double *__restrict__ rv = I.r;
+  double *__restrict__ zv = I.z;
+  const double *__restrict__ p = I.p;
+  const double *__restrict__ Ap = I.Ap;
+  const double *__restrict__ kinv = I.kinv;
   double acc[2] = {0.0, 0.0};  // z.z, r.z
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x) {
-    I.du[row] += alpha * I.p[row];
-    const double r = I.r[row] - alpha * I.Ap[row];
-    const double z = I.kinv[row] * r;
-    I.r[row] = r;
-    I.z[row] = z;
+    x[row] += alpha * p[row];
+    const double r = rv[row] - alpha * Ap[row];
+    const double z = kinv[row] * r;
+    rv[row] = r;
+    zv[row] = z;
     acc[0] += z * z;
     acc[1] += r * z;
   }
@@ -158,8 +172,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_pupdate(MeshDev m, const Inst
   if (cs->done) return;
   const double beta = cs->beta;
   const int nrow = m.nn * 3;
+  double *__restrict__ p = I.p;
+  const double *__restrict__ z = I.z;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x)
-    I.p[row] = I.z[row] + beta * I.p[row];
+    p[row] = z[row] + beta * p[row];
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
 

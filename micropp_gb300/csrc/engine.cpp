@@ -344,8 +344,8 @@ double Engine::slot_bytes() const {
   const double nd = nndim(), np = mesh_.np;
   double b = 8.0 * (3.0 * nd + 24.0 * mesh_.nelem + nvars());  // u, du, b, be, vars_aux
   if (precision_ == MICROPP3_FP64) b += 8.0 * (kEllPerNode * np + 5.0 * nd);
-  if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 4.0 * kEllPerNode * np;
-  if (precision_ == MICROPP3_MIXED) b += 4.0 * 6.0 * nd;
+  if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 4.0 * (kEllPerNode * np + nd);
+  if (precision_ == MICROPP3_MIXED) b += 4.0 * 5.0 * nd;
   if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 8.0 * 2.0 * 6.0 * nd + 4.0 * 5.0 * 6.0 * nd;
   return b;
 }
@@ -379,9 +379,11 @@ void Engine::ensure_slots(int n) {
       w.kinv = dalloc<double>(nd, "kinv");
       w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
     }
-    if (mixed || implicit) w.vals32 = dalloc<float>((size_t)kEllPerNode * mesh_.np, "ELL values (FP32)");
-    if (mixed) {
+    if (mixed || implicit) {
+      w.vals32 = dalloc<float>((size_t)kEllPerNode * mesh_.np, "ELL values (FP32)");
       w.kinv32 = dalloc<float>(nd, "kinv32");
+    }
+    if (mixed) {
       w.r32 = dalloc<float>(nd, "r32");
       w.z32 = dalloc<float>(nd, "z32");
       w.p32 = dalloc<float>(nd, "p32");
@@ -579,15 +581,16 @@ void Engine::cg_solve(const std::vector<int> &slots) {
   }
 }
 
-// The mixed form's CG: FP32 values and vectors, FP64 dot products, same iteration and stop rule.
-void Engine::cg_solve32(const std::vector<int> &slots) {
+// The mixed form's CG: FP32 values and vectors, FP64 dot products, same iteration and stop rule, with a
+// relative tolerance per slot.
+void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols) {
   const int n = (int)slots.size();
-  for (int s : slots) {
+  for (int a = 0; a < n; ++a) {
     CgState c{};
     c.min_err = cg_abs_tol_;
-    c.rel_err = cg_rel_tol_;
+    c.rel_err = rel_tols[a];
     c.max_its = cg_max_its_;
-    check(cudaMemcpyAsync(slots_[s].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
+    check(cudaMemcpyAsync(slots_[slots[a]].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
   }
   launches_ += 1;
   check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
@@ -757,7 +760,16 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     timer_end(t_asm_);
     launches_ += 1;
     if (mixed) {
-      cg_solve32(active);
+      // Inexact Newton: the FP64 residual corrects each FP32 solve, so a correction only needs to gain the
+      // digits still missing to the Newton tolerance: eta = 0.05 * nr_rel_tol * |b0| / |b_k|, kept within
+      // [cg_rel_tol, 0.1].
+      std::vector<double> eta(active.size());
+      for (size_t a = 0; a < active.size(); ++a) {
+        const int i = idx[a];
+        const double want = (norm[i] > 0) ? 0.05 * nr_rel_tol_ * norm0[i] / norm[i] : cg_rel_tol_;
+        eta[a] = std::max(cg_rel_tol_, std::min(0.1, want));
+      }
+      cg_solve32(active, eta);
       check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
     } else {
       cg_solve(active);

@@ -123,7 +123,7 @@ class Engine {
   void download_out();
   void residual(const std::vector<int> &slots);
   void cg_solve(const std::vector<int> &slots);
-  void cg_solve32(const std::vector<int> &slots);
+  void cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols);
   std::vector<int> tangent_solve(const std::vector<int> &slots);
   double slot_bytes() const;
   std::vector<NewtonResult> newton(const std::vector<int> &slots, const std::vector<std::array<double, 6>> &strains);

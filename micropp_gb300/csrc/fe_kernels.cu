@@ -66,21 +66,24 @@ __global__ void k_set_bc(MeshDev m, const Inst *insts, const int *list) {
   } else {
     c[0] = i * m.dx; c[1] = j * m.dy; c[2] = 0;
   }
-  const double *e = I.strain;
+  const double e[6] = {I.strain[0], I.strain[1], I.strain[2], I.strain[3], I.strain[4], I.strain[5]};
   const double et[3][3] = {{e[0], 0.5 * e[3], 0.5 * e[4]}, {0.5 * e[3], e[1], 0.5 * e[5]}, {0.5 * e[4], 0.5 * e[5], e[2]}};
+  double *__restrict__ u = I.u;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     double t = 0.0;
 #pragma unroll
     for (int b = 0; b < 3; ++b) t += et[a][b] * c[b];
-    I.u[n * 3 + a] = t;
+    u[n * 3 + a] = t;
   }
 }
 
 // u += du over all unknowns (solve.cpp:73).
 __global__ void k_add_du(int nndim, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x) I.u[t] += I.du[t];
+  double *__restrict__ u = I.u;
+  const double *__restrict__ du = I.du;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x) u[t] += du[t];
 }
 
 // dst = src for the listed instances; src/dst selected by `which` (0: u <- u_n, 1: u_k <- u).
@@ -141,8 +144,9 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, c
 #pragma unroll
       for (int v = 0; v < 6; ++v) aux[v] += s[v] * wg;
     }
+    double *__restrict__ bev = I.be;
 #pragma unroll
-    for (int i = 0; i < 24; ++i) I.be[(size_t)i * m.nelem + e] = be[i];
+    for (int i = 0; i < 24; ++i) bev[(size_t)i * m.nelem + e] = be[i];
   }
   double tot[6];
   const int nb = gridDim.x;
@@ -166,6 +170,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_node_rhs(MeshDev m, const Inst *
   if (n < m.nn) {
     const int i = n % m.nx, j = (n / m.nx) % m.ny, k = n / m.nxny;
     double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    const double *__restrict__ be = I.be;
+    double *__restrict__ b = I.b;
     if (!is_boundary(m, i, j, k)) {
 #pragma unroll
       for (int dz = -1; dz <= 0; ++dz)
@@ -175,17 +181,17 @@ __global__ void __launch_bounds__(kNodeBlock) k_node_rhs(MeshDev m, const Inst *
           for (int dx = -1; dx <= 0; ++dx) {
             const int e = ((k + dz) * m.ney + (j + dy)) * m.nex + (i + dx);
             const int a = local_of(-dx, -dy, -dz);
-            b0 += I.be[(size_t)(a * 3 + 0) * m.nelem + e];
-            b1 += I.be[(size_t)(a * 3 + 1) * m.nelem + e];
-            b2 += I.be[(size_t)(a * 3 + 2) * m.nelem + e];
+            b0 += be[(size_t)(a * 3 + 0) * m.nelem + e];
+            b1 += be[(size_t)(a * 3 + 1) * m.nelem + e];
+            b2 += be[(size_t)(a * 3 + 2) * m.nelem + e];
           }
       b0 = -b0;
       b1 = -b1;
       b2 = -b2;
     }
-    I.b[n * 3 + 0] = b0;
-    I.b[n * 3 + 1] = b1;
-    I.b[n * 3 + 2] = b2;
+    b[n * 3 + 0] = b0;
+    b[n * 3 + 1] = b1;
+    b[n * 3 + 2] = b2;
     sq[0] = b0 * b0 + b1 * b1 + b2 * b2;
   }
   double tot[1];
@@ -222,8 +228,9 @@ __device__ __forceinline__ float *ell_values<float>(const Inst &I) {
   return I.vals32;
 }
 
-// T = double: the plain FP64 Jacobian.  T = float: the mixed form's FP32 Jacobian -- the Gauss-point tangents
-// are still formed in FP64 (forward differences need it) and rounded once; Ke is accumulated in FP32.
+// T = double: the plain FP64 Jacobian with the reference's forward-difference tangents.  T = float: the mixed
+// form's FP32 Jacobian -- the Gauss-point tangents are formed in closed form in FP64 and rounded once; Ke is
+// accumulated in FP32.
 template <typename T>
 __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mats, const int8_t *etype,
                                                               const double *dsh_g, const T *ke_phase,
@@ -259,7 +266,11 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
   if (nonlin && p < 8) {
     double eps[6], C[36];
     gp_strain(&dsh[p * 24], ue[el], eps);
-    law_ctan(mats.m[ph], eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr, C);
+    const double *vg = I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr;
+    if constexpr (sizeof(T) == sizeof(float))
+      law_ctan_exact(mats.m[ph], eps, vg, C);  // mixed form: closed-form consistent tangent
+    else
+      law_ctan(mats.m[ph], eps, vg, C);  // FP64 form: the reference's forward differences
 #pragma unroll
     for (int i = 0; i < 36; ++i) Cg[el][p][i] = (T)C[i];
   }

@@ -132,6 +132,97 @@ __device__ __forceinline__ void law_ctan(const MatDev &m, const double *eps, con
   }
 }
 
+// Consistent tangent d(sigma)/d(eps) of the three laws in closed form -- the derivative that the reference's
+// forward differences (apply_perturbation, material.cpp:48-63) approximate.  Used by the mixed form's Jacobian
+// and by the implicit ctan, where it is both exact and far cheaper than 7 stress evaluations in FP64.
+//  damage, unloading (r <= r_old_a): (1 - D_old) C
+//  damage, loading:                  (q/r) C + (q' - q/r) / r^2 * s (x) s,   s = C eps, r = sqrt(s . eps)
+//  J2, plastic:  D + K 1(x)1 - 2 mu [ n (x) (D n) / den + (dl / |s|) (I - n (x) n) D ]
+//                with D = d(s_trial)/d(eps), n = s_trial / |s_trial| (the reference's Voigt norm),
+//                dl = f / den, den = 2 mu (1 + Ka / (3 mu))
+__device__ __forceinline__ void law_ctan_exact(const MatDev &m, const double *eps, const double *vars, double *C) {
+  // elastic C (material.cpp:84-95)
+#pragma unroll
+  for (int i = 0; i < 36; ++i) C[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i * 6 + j] = m.lambda;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) C[i * 6 + i] += m.two_mu;
+#pragma unroll
+  for (int i = 3; i < 6; ++i) C[i * 6 + i] = m.mu;
+  if (m.type == 0) return;
+  if (m.type == 2) {
+    double s[6];
+    law_elastic(m, eps, s);
+    double product = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) product += s[i] * eps[i];
+    const double r = (product >= 0) ? sqrt(product) : 0.0;
+    const double r_old = vars ? vars[0] : 0.0;
+    const double D_old = vars ? vars[1] : 0.0;
+    const double r_old_a = (r_old < m.xt_thr) ? m.xt_thr : r_old;
+    if (r <= r_old_a) {
+      const double f = 1 - D_old;
+#pragma unroll
+      for (int i = 0; i < 36; ++i) C[i] *= f;
+      return;
+    }
+    const double q = law_damage_hardening(m, r);
+    const double qp = (r < m.dmg_r0) ? 0.0 : (r < m.dmg_r1 ? 10.0 : 5.0);
+    const double a = q / r;
+    const double b = (qp - a) / (r * r);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) C[i * 6 + j] = a * C[i * 6 + j] + b * s[i] * s[j];
+    return;
+  }
+  // J2
+  double dl, n[6], st[6];
+  const bool plastic = law_j2_trial(m, eps, vars, &dl, n, st);
+  // D = d(s_trial)/d(eps): 2 mu (I - 1/3 1(x)1) on the normal block, mu on the shear diagonal
+  double D[36];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) D[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) D[i * 6 + j] = m.two_mu * ((i == j ? 1.0 : 0.0) - 1.0 / 3.0);
+#pragma unroll
+  for (int i = 3; i < 6; ++i) D[i * 6 + i] = m.mu;
+#pragma unroll
+  for (int i = 0; i < 36; ++i) C[i] = D[i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i * 6 + j] += m.k;
+  if (!plastic) return;
+  double snorm = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) snorm += st[i] * st[i];
+  snorm = sqrt(snorm);
+  double Dn[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t += n[i] * D[i * 6 + j];
+    Dn[j] = t;
+  }
+  const double c1 = m.two_mu / m.pl_den;
+  const double c2 = m.two_mu * dl / snorm;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      // (I - n n^T) D row i, column j = D_ij - n_i (n^T D)_j
+      const double proj = D[i * 6 + j] - n[i] * Dn[j];
+      C[i * 6 + j] -= c1 * n[i] * Dn[j] + c2 * proj;
+    }
+}
+
 // evolute (material.cpp:97-100, 168-181, 291-302): history update, returns the nonlinear flag.  J2 writes
 // only when the old history exists; damage always writes (r, D).
 __device__ __forceinline__ bool law_evolve(const MatDev &m, const double *eps, const double *vold, bool has_old,

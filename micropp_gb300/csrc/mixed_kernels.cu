@@ -80,17 +80,24 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
   if (n < m.nn) {
     int i, j, k;
     const bool b = bnd(m, n, i, j, k);
+    const float *__restrict__ vals = I.vals32;
+    const double *__restrict__ bb = I.b;
+    float *__restrict__ kinv = I.kinv32;
+    float *__restrict__ du = I.du32;
+    float *__restrict__ rv = I.r32;
+    float *__restrict__ zv = I.z32;
+    float *__restrict__ pv = I.p32;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int row = n * 3 + d;
-      const float kd = b ? 1.0f : 1.0f / I.vals32[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
-      const float r = (float)I.b[row];
+      const float kd = b ? 1.0f : 1.0f / vals[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+      const float r = (float)bb[row];
       const float z = kd * r;
-      I.kinv32[row] = kd;
-      I.du32[row] = 0.0f;
-      I.r32[row] = r;
-      I.z32[row] = z;
-      I.p32[row] = z;
+      kinv[row] = kd;
+      du[row] = 0.0f;
+      rv[row] = r;
+      zv[row] = z;
+      pv[row] = z;
       acc[0] += (double)r * (double)z;
       acc[1] += (double)z * (double)z;
     }
@@ -119,11 +126,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_spmv(MeshDev m, const Inst 
   if (n < m.nn) {
     int i, j, k;
     const float *__restrict__ p = I.p32;
+    float *__restrict__ Ap = I.Ap32;
     if (bnd(m, n, i, j, k)) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const float pv = p[n * 3 + d];
-        I.Ap32[n * 3 + d] = pv;
+        Ap[n * 3 + d] = pv;
         acc[0] += (double)pv * (double)pv;
       }
     } else {
@@ -145,9 +153,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_spmv(MeshDev m, const Inst 
         y2 = fmaf(__ldcs(vs + 7 * np), x1, y2);
         y2 = fmaf(__ldcs(vs + 8 * np), x2, y2);
       }
-      I.Ap32[n * 3 + 0] = y0;
-      I.Ap32[n * 3 + 1] = y1;
-      I.Ap32[n * 3 + 2] = y2;
+      Ap[n * 3 + 0] = y0;
+      Ap[n * 3 + 1] = y1;
+      Ap[n * 3 + 2] = y2;
       acc[0] = (double)(p[n * 3 + 0] * y0 + p[n * 3 + 1] * y1 + p[n * 3 + 2] * y2);
     }
   }
@@ -165,13 +173,19 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Ins
   if (cs->done) return;
   const float alpha = (float)cs->alpha;
   const int nrow = m.nn * 3;
+  float *__restrict__ du = I.du32;
+  float *__restrict__ rv = I.r32;
+  float *__restrict__ zv = I.z32;
+  const float *__restrict__ p = I.p32;
+  const float *__restrict__ Ap = I.Ap32;
+  const float *__restrict__ kinv = I.kinv32;
   double acc[2] = {0.0, 0.0};
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x) {
-    I.du32[row] = fmaf(alpha, I.p32[row], I.du32[row]);
-    const float r = fmaf(-alpha, I.Ap32[row], I.r32[row]);
-    const float z = I.kinv32[row] * r;
-    I.r32[row] = r;
-    I.z32[row] = z;
+    du[row] = fmaf(alpha, p[row], du[row]);
+    const float r = fmaf(-alpha, Ap[row], rv[row]);
+    const float z = kinv[row] * r;
+    rv[row] = r;
+    zv[row] = z;
     acc[0] += (double)(z * z);
     acc[1] += (double)(r * z);
   }
@@ -201,15 +215,18 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_pupdate(MeshDev m, const In
   if (cs->done) return;
   const float beta = (float)cs->beta;
   const int nrow = m.nn * 3;
+  float *__restrict__ p = I.p32;
+  const float *__restrict__ z = I.z32;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x)
-    I.p32[row] = fmaf(beta, I.p32[row], I.z32[row]);
+    p[row] = fmaf(beta, p[row], z[row]);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
 
 __global__ void k_add_du32(int nndim, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x)
-    I.u[t] += (double)I.du32[t];
+  double *__restrict__ u = I.u;
+  const float *__restrict__ du = I.du32;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x) u[t] += (double)du[t];
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -247,15 +264,23 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
         }
       }
     }
+    double *__restrict__ F6 = I.F6;
+    double *__restrict__ X6 = I.X6;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const size_t idx = ((size_t)n * 6 + r) * 3 + d;
-        I.F6[idx] = f[r][d];
-        I.X6[idx] = 0.0;
+        F6[idx] = f[r][d];
+        X6[idx] = 0.0;
         acc[r] += f[r][d] * f[r][d];
       }
+    // Jacobi inverse of the tangent for the 6-RHS CG (boundary rows are identity rows)
+    float *__restrict__ kinv = I.kinv32;
+    const bool b = bnd(m, n, i, j, k);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      kinv[n * 3 + d] = b ? 1.0f : 1.0f / I.vals32[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
   }
   double tot[6];
   if (grid_sum<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
@@ -280,7 +305,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
       for (int d = 0; d < 3; ++d) rf[r][d] = b ? 0.0 : I.F6[((size_t)n * 6 + r) * 3 + d];
     float kd[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) kd[d] = b ? 1.0f : 1.0f / I.vals32[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+    for (int d = 0; d < 3; ++d) kd[d] = I.kinv32[n * 3 + d];
     if (!b) {
       const float *__restrict__ v = I.vals32 + n;
       const size_t np = m.np;
@@ -299,6 +324,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
         }
       }
     }
+    float *__restrict__ R6 = I.R6;
+    float *__restrict__ Z6 = I.Z6;
+    float *__restrict__ P6 = I.P6;
+    float *__restrict__ D6 = I.D6;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -306,10 +335,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
         const size_t idx = ((size_t)n * 6 + r) * 3 + d;
         const float rr = (float)rf[r][d];
         const float z = kd[d] * rr;
-        I.R6[idx] = rr;
-        I.Z6[idx] = z;
-        I.P6[idx] = z;
-        I.D6[idx] = 0.0f;
+        R6[idx] = rr;
+        Z6[idx] = z;
+        P6[idx] = z;
+        D6[idx] = 0.0f;
         acc[r] += (double)rr * (double)z;
         acc[6 + r] += (double)z * (double)z;
         acc[12 + r] += rf[r][d] * rf[r][d];
@@ -380,7 +409,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_spmv(MeshDev m, const Inst *
           }
       }
     }
-    float2 *ap2 = reinterpret_cast<float2 *>(I.AP6 + (size_t)n * 18);
+    float2 *__restrict__ ap2 = reinterpret_cast<float2 *>(I.AP6 + (size_t)n * 18);
     const float2 *p2 = reinterpret_cast<const float2 *>(P + (size_t)n * 18);
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
@@ -408,22 +437,26 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
   double acc[12];
 #pragma unroll
   for (int q = 0; q < 12; ++q) acc[q] = 0.0;  // [0,6): z.z  [6,12): r.z
+  float *__restrict__ D6 = I.D6;
+  float *__restrict__ R6 = I.R6;
+  float *__restrict__ Z6 = I.Z6;
+  const float *__restrict__ P6 = I.P6;
+  const float *__restrict__ AP6 = I.AP6;
+  const float *__restrict__ kinv = I.kinv32;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x) {
-    int i, j, k;
-    const bool b = bnd(m, n, i, j, k);
     float kd[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) kd[d] = b ? 1.0f : 1.0f / I.vals32[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+    for (int d = 0; d < 3; ++d) kd[d] = kinv[n * 3 + d];
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const size_t idx = ((size_t)n * 6 + r) * 3 + d;
-        I.D6[idx] = fmaf(alpha[r], I.P6[idx], I.D6[idx]);
-        const float rr = fmaf(-alpha[r], I.AP6[idx], I.R6[idx]);
+        D6[idx] = fmaf(alpha[r], P6[idx], D6[idx]);
+        const float rr = fmaf(-alpha[r], AP6[idx], R6[idx]);
         const float z = kd[d] * rr;
-        I.R6[idx] = rr;
-        I.Z6[idx] = z;
+        R6[idx] = rr;
+        Z6[idx] = z;
         acc[r] += (double)(z * z);
         acc[6 + r] += (double)(rr * z);
       }
@@ -460,10 +493,18 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_pupdate(MeshDev m, const Ins
     beta[r] = (float)cs->beta[r];
     live[r] = !cs->done[r];
   }
-  const size_t total = (size_t)m.nn * 18;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-    const int r = (int)((t / 3) % 6);
-    if (live[r]) I.P6[t] = fmaf(beta[r], I.P6[t], I.Z6[t]);
+  float *__restrict__ P6 = I.P6;
+  const float *__restrict__ Z6 = I.Z6;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      if (!live[r]) continue;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const size_t idx = ((size_t)n * 6 + r) * 3 + d;
+        P6[idx] = fmaf(beta[r], P6[idx], Z6[idx]);
+      }
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
@@ -472,8 +513,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_pupdate(MeshDev m, const Ins
 __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const size_t total = (size_t)m.nn * 18;
+  double *__restrict__ X6 = I.X6;
+  const float *__restrict__ D6 = I.D6;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
-    I.X6[t] += (double)I.D6[t];
+    X6[t] += (double)D6[t];
 }
 
 // ctan[v][i] = (1/V) sum over Gauss points of wg (C_gp B (w_i + x_i))_v, one thread per Gauss point, FP64.
@@ -520,7 +563,7 @@ __global__ void __launch_bounds__(128) k_ctan_avg(MeshDev m, Mats mats, const in
       }
       eps[0] = e0; eps[1] = e1; eps[2] = e2; eps[3] = e3; eps[4] = e4; eps[5] = e5;
     }
-    law_ctan(mat, eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr, C);
+    law_ctan_exact(mat, eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr, C);
 #pragma unroll 1
     for (int r = 0; r < 6; ++r) {
       double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
@@ -623,15 +666,14 @@ int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, in
 
 int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_update<<<dim3(cdiv(m->nn, kNodeBlock * 2), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg6_update<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_pupdate(const MeshDev *m, const Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_pupdate<<<dim3(cdiv((size_t)m->nn * 18, kNodeBlock * 8), nlist), kNodeBlock, 0, s>>>(*m, insts, list,
-                                                                                            active_count);
+  k_cg6_pupdate<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
   return (int)cudaGetLastError();
 }
 
