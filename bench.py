@@ -33,10 +33,11 @@ sys.path.insert(0, ROOT)
 METRIC = "RVE homogenizations/s (stress+ctan) at 60^3, adjoint+batched vs plain, 1 GB300"
 UNIT = "homogenizations/s"
 
-# Measured on a GB300 with this workload (n = 60, seeds below): CG iterations and Newton iterations of one
-# stress+ctan homogenization, averaged over the 32 RVEs.  The GPU arm prints its own figures every run; the
-# reference arm converts its bounded sample (one Newton iteration per RVE) into homogenizations/s with them.
-CG_ITS_PER_HOM = {60: None}
+# CG iterations of one stress+ctan homogenization by the reference algorithm (the plain form), averaged over
+# the 32 RVEs of the default workload (n = 60, seed 2024), as measured on a GB300.  The GPU arm measures its
+# own figure every run; the reference arm converts its bounded CPU sample (one Newton iteration per RVE) into
+# homogenizations/s with this one.
+CG_ITS_PER_HOM = {60: 1588.1}
 
 
 def parse():
@@ -74,16 +75,22 @@ def workload(n, rves, seed, rank):
 # perturbed Newton solves).  fast: FP32 Jacobian and CG inside FP64 refinement, Newton converged to 1e-8 of the
 # initial residual (average stress within 1e-7 of the converged FP64 solution), ctan by implicit
 # differentiation (one 6-RHS tangent solve).
+# `batched`: all RVEs are Gauss points of one handle, homogenized together by one micropp3_homogenize call
+# (lockstep Newton and CG over the batch with per-RVE convergence masks); otherwise each RVE has its own
+# handle and they are homogenized one after the other, as a macro code calls one micro point at a time.
+# plain_batched (not in the default run) is the plain algorithm with batching alone.
 FORMS = {
-    "plain": dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5),
-    "fast": dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8),
+    "plain": dict(batched=False, cfg=dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5)),
+    "fast": dict(batched=True, cfg=dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8)),
+    "plain_batched": dict(batched=True, cfg=dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5)),
 }
 
 
-def gpu_config(n, et, xt, form="plain"):
+def gpu_config(n, et, xt, form="plain", ngp=1):
     import micropp_gb300 as mg
     mats = [mg.material(2, 1e7, 0.25, 0, 0, xt), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
-    return mg.config(n, mats=mats, coupling=[2], elem_type=et, lin_stress=0, calc_ctan_lin=0, **FORMS[form])
+    return mg.config(n, ngp=ngp, mats=mats, coupling=[2] * ngp, elem_type=et, lin_stress=0, calc_ctan_lin=0,
+                     **FORMS[form]["cfg"])
 
 
 # ---------------------------------------------------------------------------------------------------------
@@ -253,9 +260,11 @@ def run_reference(args):
     }))
 
 
-def load_traffic(n, family="spmv", fp32=False):
-    """DRAM bytes per launch of the kernel from a committed ncu summary (profiles/*_traffic.json), if any."""
+def load_traffic(n, family="spmv", fp32=False, sym=False):
+    """DRAM bytes of one RVE's launch of the kernel from a committed ncu summary (profiles/*_traffic.json)."""
     name = {("spmv", False): "spmv_fp64", ("spmv", True): "spmv_fp32", ("spmv6", True): "spmv6_fp32"}.get((family, fp32))
+    if name and fp32 and sym:
+        name += "_sym"
     p = os.path.join(ROOT, "profiles", f"{name}_traffic.json") if name else ""
     if name and os.path.exists(p):
         d = json.load(open(p))
@@ -269,18 +278,36 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
 
     import micropp_gb300 as mg
     n, R = args.size, args.rves
-    handles = [mg.Micropp(gpu_config(n, et, float(xts[i]), form)) for i in range(R)]
+    batched = FORMS[form]["batched"]
+    if batched:
+        # one handle, RVE i = Gauss point i (the RVEs share materials and microstructure)
+        handles = [mg.Micropp(gpu_config(n, et, float(xts[0]), form, ngp=R))]
+        points = [(handles[0], i) for i in range(R)]
+    else:
+        handles = [mg.Micropp(gpu_config(n, et, float(xts[i]), form)) for i in range(R)]
+        points = [(h, 0) for h in handles]
     # Set-up: load each RVE to half its target and accept the step; grow the target until it is nonlinear.
     tg = [t.copy() for t in targets]
-    for i, h in enumerate(handles):
-        for _ in range(4):
-            h.set_strain(0, 0.5 * tg[i])
+    pending = list(range(R))
+    for _ in range(4):
+        for i in pending:
+            h, gp = points[i]
+            h.set_strain(gp, 0.5 * tg[i])
+        for h in {id(points[i][0]): points[i][0] for i in pending}.values():
             h.homogenize()
-            if h.is_non_linear(0):
-                break
-            tg[i] *= 1.5
+        still = []
+        for i in pending:
+            h, gp = points[i]
+            if not h.is_non_linear(gp):
+                tg[i] *= 1.5
+                still.append(i)
+        if not still:
+            break
+        pending = still
+    for h in handles:
         h.update_vars()
-    nonlinear = sum(h.is_non_linear(0) for h in handles)
+    nonlinear = sum(h.is_non_linear(gp) for h, gp in points)
+    sym32 = handles[0].ell32_symmetric()
     strain_bufs = [np.ascontiguousarray(t, dtype=np.float64) for t in tg]
     out_s = np.zeros((R, 6))
     out_c = np.zeros((R, 36))
@@ -288,6 +315,16 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
 
     def step(k):
         dev_ms = 0.0
+        if batched:
+            h = handles[0]
+            for i in range(R):
+                e = strain_bufs[i] * (1.0 + 1e-3 * k)
+                L.micropp3_set_strain(ctypes.byref(h.h), i, dp(e))
+            L.micropp3_homogenize(ctypes.byref(h.h))
+            for i in range(R):
+                L.micropp3_get_stress(ctypes.byref(h.h), i, dp(out_s[i]))
+                L.micropp3_get_ctan(ctypes.byref(h.h), i, dp(out_c[i]))
+            return L.micropp3_last_homogenize_ms(ctypes.byref(h.h))
         for i, h in enumerate(handles):
             e = strain_bufs[i] * (1.0 + 1e-3 * k)
             L.micropp3_set_strain(ctypes.byref(h.h), 0, dp(e))
@@ -315,10 +352,11 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     launches = sum(h.kernel_launches() for h in handles) - l0
     if L.micropp3_last_error():
         raise RuntimeError(L.micropp3_last_error().decode())
-    status = [h.status(0) for h in handles]
+    status = [h.status(gp) for h, gp in points]
+    newton = [h.newton(gp) for h, gp in points]  # (Newton its, CG its, converged) of the last solve
     finite = bool(np.isfinite(out_s).all() and np.isfinite(out_c).all())
     stats = {}
-    for fam in ("spmv", "spmv6", "cg_update", "assembly", "residual"):
+    for fam in ("spmv", "spmv6", "cg_update", "cg6_update", "assembly", "residual"):
         tot = [h.kernel_stats(fam) for h in handles]
         stats[fam] = (sum(t[0] for t in tot), sum(t[1] for t in tot), sum(t[2] for t in tot))
     for h in handles:
@@ -326,29 +364,38 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     dev_s = max_over_ranks(pg, dev_ms / 1e3, world)
     wall_s = max_over_ranks(pg, wall, world)
     homs = R * args.steps * world
-    return {"form": form, "value": homs / dev_s, "e2e": homs / wall_s, "dev_s": dev_s, "wall_s": wall_s,
-            "cg_its": cg_its, "launches": launches, "stats": stats, "clocks": clk.summary(),
-            "nonlinear": nonlinear, "status": status, "finite": finite, "stress": out_s.copy(), "ctan": out_c.copy()}
+    return {"form": form, "batched": batched, "sym32": sym32, "value": homs / dev_s, "e2e": homs / wall_s, "dev_s": dev_s,
+            "wall_s": wall_s, "cg_its": cg_its, "launches": launches, "stats": stats, "clocks": clk.summary(),
+            "nonlinear": nonlinear, "status": status, "newton": newton, "finite": finite, "stress": out_s.copy(),
+            "ctan": out_c.copy()}
 
 
 def roofline_of(res, n, peak, peak_kind):
     """Roofline record of the form's dominant linear-algebra kernel (most device time)."""
     nrow = 3 * (n + 1) ** 3
-    fp32 = res["form"] == "fast"
+    fp32 = FORMS[res["form"]]["cfg"]["precision"] == 1
     cands = {"spmv": res["stats"]["spmv"], "spmv6": res["stats"]["spmv6"]}
     fam = max(cands, key=lambda k: cands[k][1])
     nk, ms, by = cands[fam]
     achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
+    # algorithmic bytes of one RVE's SpMV: the stored values once (81 per row, or 42 per row for the symmetric
+    # half), x read once, y written once (per right-hand side)
+    vpr = 42 if res.get("sym32") else 81
+    store = "symmetric half" if res.get("sym32") else "full stencil"
     if fam == "spmv6":
-        name, per = "k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides)", nrow * (81 * 4 + 12 * 4)
+        name, per = f"k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides, {store})", nrow * (vpr * 4 + 12 * 4)
     elif fp32:
-        name, per = "k_cg32_spmv (FP32 ELL SpMV + p.Ap)", nrow * (81 * 4 + 2 * 4)
+        name, per = f"k_cg32_spmv (FP32 ELL SpMV + p.Ap, {store})", nrow * (vpr * 4 + 2 * 4)
     else:
         name, per = "k_cg_spmv (FP64 ELL SpMV + p.Ap)", nrow * (81 * 8 + 2 * 8)
-    traffic = load_traffic(n, fam, fp32)
+    rves_per_launch = by / nk / per if nk else None
+    traffic = load_traffic(n, fam, fp32, bool(res.get("sym32")))  # DRAM bytes of one RVE's SpMV (ncu)
+    if traffic is not None and rves_per_launch:
+        traffic *= rves_per_launch
     return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": per, "launches": nk, "avg_us": 1e3 * ms / nk if nk else None}
+            "algorithmic_bytes_per_launch": by / nk if nk else None, "algorithmic_bytes_per_rve": per,
+            "rves_per_launch": rves_per_launch, "launches": nk, "avg_us": 1e3 * ms / nk if nk else None}
 
 
 def run_gpu(args):
@@ -389,12 +436,16 @@ def run_gpu(args):
                               f"(the plain form, measured in this run)")}
 
     def form_record(r):
-        return {"value": r["value"], "e2e": r["e2e"], "ms_per_step": 1e3 * r["dev_s"] / args.steps,
+        return {"value": r["value"], "e2e": r["e2e"], "batched": r["batched"],
+                "ms_per_step": 1e3 * r["dev_s"] / args.steps,
                 "cg_its_per_homogenization": r["cg_its"] / (R * args.steps),
                 "cg_its_per_s": r["cg_its"] * world / r["dev_s"],
                 "dof_updates_per_s": r["cg_its"] * nrow * world / r["dev_s"],
                 "nonlinear_rves": r["nonlinear"], "finite": r["finite"],
                 "status_counts": {str(k): r["status"].count(k) for k in sorted(set(r["status"]))},
+                "newton_its_mean_max": [float(np.mean([x[0] for x in r["newton"]])), max(x[0] for x in r["newton"])],
+                "newton_cg_its_mean_max": [float(np.mean([x[1] for x in r["newton"]])),
+                                           max(x[1] for x in r["newton"])],
                 "gpu_launches": r["launches"], "roofline": roofline_of(r, n, peak, peak_kind),
                 "kernels": {k: {"launches": v[0], "ms": v[1], "avg_us": 1e3 * v[1] / v[0] if v[0] else None,
                                 "algorithmic_GBps": v[2] / (v[1] / 1e3) / 1e9 if v[1] else None}
@@ -409,7 +460,7 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * head["dev_s"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if head["form"] == "fast" else "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if FORMS[head["form"]]["cfg"]["precision"] == 1 else "f64",
         "data": "synthetic",
         "config": {"workload": f"{R} damage RVEs of {n}^3 per GPU (4 layers normal to z, Xt=1e5), "
                                f"FE_FULL stress+ctan, one homogenization per RVE per step",

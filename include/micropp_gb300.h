@@ -104,7 +104,8 @@ double micropp3_last_homogenize_ms(const struct micropp3 *self);
 
 /* Kernel timing.  When enabled, every launch of the named kernel family is bracketed by CUDA events on the
  * launching stream; micropp3_kernel_stats returns the launch count, the summed device time (ms) and the
- * algorithmic bytes moved by those launches.  Families: "spmv", "cg_update", "assembly", "residual". */
+ * algorithmic bytes moved by those launches.  Families: "spmv" (the Newton CG's SpMV), "cg_update" (its two
+ * vector kernels), "spmv6" and "cg6_update" (the same for the 6-RHS tangent CG), "assembly", "residual". */
 void micropp3_set_kernel_timing(struct micropp3 *self, int enable);
 int micropp3_kernel_stats(const struct micropp3 *self, const char *family, long *launches, double *ms,
                           double *bytes);
@@ -139,6 +140,11 @@ int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, cons
 /* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
 long micropp3_total_cg_its(const struct micropp3 *self);
 long micropp3_kernel_launches(const struct micropp3 *self);
+
+/* 1 when the handle's FP32 Jacobian (mixed precision or implicit ctan) is stored as its symmetric half: every
+ * phase has a symmetric consistent tangent (elastic, damage).  0 for the full stencil (a J2 phase, or no
+ * FP32 Jacobian). */
+int micropp3_ell32_symmetric(const struct micropp3 *self);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,8 @@
 
 namespace mgb {
 
+constexpr int kUpdRows = 4;  // rows per thread of the vector update
+
 __device__ __forceinline__ bool node_boundary(const MeshDev &m, int n, int &i, int &j, int &k) {
   i = n % m.nx;
   j = (n / m.nx) % m.ny;
@@ -136,14 +138,30 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_update(MeshDev m, const Inst 
   const double *__restrict__ Ap = I.Ap;
   const double *__restrict__ kinv = I.kinv;
   double acc[2] = {0.0, 0.0};  // z.z, r.z
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x) {
-    x[row] += alpha * p[row];
-    const double r = rv[row] - alpha * Ap[row];
-    const double z = kinv[row] * r;
-    rv[row] = r;
-    zv[row] = z;
-    acc[0] += z * z;
-    acc[1] += r * z;
+  // kUpdRows rows per thread, strided by the grid so that every load is coalesced; all loads first.
+  const int stride = gridDim.x * blockDim.x;
+  for (int row0 = blockIdx.x * blockDim.x + threadIdx.x; row0 < nrow; row0 += kUpdRows * stride) {
+    double pv[kUpdRows], av[kUpdRows], rr[kUpdRows], xv[kUpdRows], kv[kUpdRows];
+#pragma unroll
+    for (int q = 0; q < kUpdRows; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) {
+        pv[q] = p[row]; av[q] = Ap[row]; rr[q] = rv[row]; xv[q] = x[row]; kv[q] = kinv[row];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kUpdRows; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) {
+        x[row] = xv[q] + alpha * pv[q];
+        const double r = rr[q] - alpha * av[q];
+        const double z = kv[q] * r;
+        rv[row] = r;
+        zv[row] = z;
+        acc[0] += z * z;
+        acc[1] += r * z;
+      }
+    }
   }
   double tot[2];
   if (grid_sum<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
@@ -213,7 +231,8 @@ int mgb_launch_cg_spmv(const MeshDev *m, const Inst *insts, const int *list, int
 
 int mgb_launch_cg_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg_update<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg_update<<<dim3(cdiv((size_t)m->nn * 3, (size_t)kUpdRows * kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts,
+                                                                                                      list);
   return (int)cudaGetLastError();
 }
 

@@ -12,12 +12,23 @@
 //                                            implicit; boundary rows are identity rows and are not stored.
 //   element residual blocks be               24 * nelem doubles, [(a*3+d) * nelem + e]
 //   internal variables                       7 doubles per Gauss point, [(e*8 + g)*7 + v] (params.hpp:41)
-// Mixed form: the same ELL layout in FP32 (vals32) with FP32 CG vectors; the six tangent right-hand sides
-// of the implicit ctan are stored node-major, [(n*6 + i)*3 + d] (18 values per node), so one thread reads a
-// node's 6 x 3 block contiguously.
+// Mixed form: the same ELL layout in FP32 (vals32) with FP32 CG vectors.  When every phase has a symmetric
+// tangent (elastic, damage), vals32 holds only the 14 "upper" stencil slots s = 13..26 (self and the
+// neighbours after it in (dz,dy,dx) order) at [((s-13)*9 + fi*3 + fj) * np + n], for every node including
+// boundary nodes; the block of a lower slot s of node n is the transpose of slot 26-s of its neighbour.
+// The rest of the mixed form: the six tangent right-hand sides
+// of the implicit ctan are stored component-major, [(i*3 + d) * np + n] (18 * np values), so that a warp
+// reading one component of 32 consecutive nodes touches 128 contiguous bytes.
 #pragma once
 
+#include <stddef.h>
 #include <stdint.h>
+
+#ifdef __CUDACC__
+#define MGB_HD __host__ __device__ __forceinline__
+#else
+#define MGB_HD inline
+#endif
 
 namespace mgb {
 
@@ -29,6 +40,7 @@ constexpr int kEllPerNode = 243;  // 27 stencil nodes x 3 x 3
 struct MeshDev {
   int nx, ny, nz, nxny, nn, np;  // np: padded node stride of the ELL arrays
   int nex, ney, nez, nelem;
+  int sym32, pad_;               // 1: the FP32 ELL holds the symmetric half (see kSymSlots)
   double lx, ly, lz, dx, dy, dz, wg, vol_tot;
 };
 
@@ -87,6 +99,9 @@ struct Inst {
   InstOut *out;
   // mixed form (FP32 Jacobian and CG vectors)
   float *vals32, *kinv32, *r32, *z32, *p32, *Ap32, *du32;
+  // Gauss-point tangent descriptors of the damage law for the symmetric FP32 Jacobian, written by the FP64
+  // residual: [(q * 8 + g) * nelem + e], q = 0: a, 1: c, 2..7: s  (C_gp = a C_el + c s s^T)
+  float *gpd;
   // implicit ctan: 6 right-hand sides
   double *X6, *F6;
   float *R6, *Z6, *P6, *AP6, *D6;
@@ -99,5 +114,10 @@ struct Inst {
 constexpr int kRedStride = 40;
 constexpr int kNodeBlock = 256;
 constexpr int kElemBlock = 128;
+
+constexpr int kSymSlots = 14;
+
+// Offset of component (i, d) of a 6-RHS vector.
+MGB_HD size_t c6(int i, int d, size_t np) { return (size_t)(i * 3 + d) * np; }
 
 }  // namespace mgb

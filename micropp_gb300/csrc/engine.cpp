@@ -92,6 +92,11 @@ Engine::Engine(const micropp3_config &cfg) {
   build_elem_types(cfg);
   build_materials(cfg);
   build_phase_stiffness();
+  // The FP32 Jacobian (mixed precision or implicit ctan) is stored as its symmetric half when every phase
+  // in use has a symmetric consistent tangent (elastic, damage); a J2 phase keeps the full stencil.
+  sym32_ = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
+  for (int e = 0; e < mesh_.nelem && sym32_; ++e) sym32_ = mats_.m[etype_[e]].type != 1;
+  mesh_.sym32 = sym32_ ? 1 : 0;
 
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   check(cudaEventCreate(&ev0_), "event");
@@ -107,6 +112,12 @@ Engine::Engine(const micropp3_config &cfg) {
     for (int i = 0; i < 3 * 576; ++i) ke32[i] = (float)(&ke_phase_[0][0])[i];
     d_ke32_ = dalloc<float>(3 * 576, "ke32");
     check(cudaMemcpy(d_ke32_, ke32, sizeof(ke32), cudaMemcpyHostToDevice), "ke32 upload");
+    d_k0g32_ = dalloc<float>(k0g32_.size(), "k0g32");
+    check(cudaMemcpy(d_k0g32_, k0g32_.data(), k0g32_.size() * sizeof(float), cudaMemcpyHostToDevice), "k0g upload");
+    float dsh32[192];
+    for (int i = 0; i < 192; ++i) dsh32[i] = (float)dsh_[i];
+    d_dsh32_ = dalloc<float>(192, "dsh32");
+    check(cudaMemcpy(d_dsh32_, dsh32, sizeof(dsh32), cudaMemcpyHostToDevice), "dsh32 upload");
   }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
@@ -159,7 +170,7 @@ Engine::~Engine() {
     dfree(g.vars_k);
   }
   free_slots();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_})
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_})
     for (auto &e : t->pool) {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
@@ -168,6 +179,8 @@ Engine::~Engine() {
   dfree(d_dsh_);
   dfree(d_ke_);
   dfree(d_ke32_);
+  dfree(d_k0g32_);
+  dfree(d_dsh32_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -277,6 +290,7 @@ void Engine::build_materials(const micropp3_config &cfg) {
 // Element stiffness of an elastic phase, get_elem_mat (assembly.cpp:140-178) with the elastic ctan
 // (material.cpp:84-95).  B and wg are uniform over the mesh, so one Ke serves every element of the phase.
 void Engine::build_phase_stiffness() {
+  k0g32_.assign((size_t)3 * 8 * 576, 0.0f);
   for (int ph = 0; ph < 3; ++ph) {
     const MatDev &m = mats_.m[ph];
     double C[36] = {0};
@@ -294,11 +308,16 @@ void Engine::build_phase_stiffness() {
           for (int k = 0; k < 6; ++k) t += C[i * 6 + k] * bmat_[gp][k][j];
           cxb[i][j] = t * mesh_.wg;
         }
+      double Kg[576] = {0};
       for (int mm = 0; mm < 6; ++mm)
         for (int i = 0; i < 24; ++i) {
           const double bmi = bmat_[gp][mm][i];
-          for (int j = 0; j < 24; ++j) K[i * 24 + j] += bmi * cxb[mm][j];
+          for (int j = 0; j < 24; ++j) {
+            K[i * 24 + j] += bmi * cxb[mm][j];
+            Kg[i * 24 + j] += bmi * cxb[mm][j];
+          }
         }
+      for (int q = 0; q < 576; ++q) k0g32_[((size_t)ph * 8 + gp) * 576 + q] = (float)Kg[q];
     }
   }
 }
@@ -344,9 +363,10 @@ double Engine::slot_bytes() const {
   const double nd = nndim(), np = mesh_.np;
   double b = 8.0 * (3.0 * nd + 24.0 * mesh_.nelem + nvars());  // u, du, b, be, vars_aux
   if (precision_ == MICROPP3_FP64) b += 8.0 * (kEllPerNode * np + 5.0 * nd);
-  if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 4.0 * (kEllPerNode * np + nd);
+  if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT)
+    b += 4.0 * ((sym32_ ? kSymSlots * 9 : kEllPerNode) * np + nd + (sym32_ ? 64.0 * mesh_.nelem : 0.0));
   if (precision_ == MICROPP3_MIXED) b += 4.0 * 5.0 * nd;
-  if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += 8.0 * 2.0 * 6.0 * nd + 4.0 * 5.0 * 6.0 * nd;
+  if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += (8.0 * 2.0 + 4.0 * 5.0) * 18.0 * np;
   return b;
 }
 
@@ -380,8 +400,9 @@ void Engine::ensure_slots(int n) {
       w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
     }
     if (mixed || implicit) {
-      w.vals32 = dalloc<float>((size_t)kEllPerNode * mesh_.np, "ELL values (FP32)");
+      w.vals32 = dalloc<float>((size_t)(sym32_ ? kSymSlots * 9 : kEllPerNode) * mesh_.np, "ELL values (FP32)");
       w.kinv32 = dalloc<float>(nd, "kinv32");
+      if (sym32_) w.gpd = dalloc<float>((size_t)64 * mesh_.nelem, "Gauss-point tangent terms");
     }
     if (mixed) {
       w.r32 = dalloc<float>(nd, "r32");
@@ -391,13 +412,14 @@ void Engine::ensure_slots(int n) {
       w.du32 = dalloc<float>(nd, "du32");
     }
     if (implicit) {
-      w.X6 = dalloc<double>(6 * nd, "X6");
-      w.F6 = dalloc<double>(6 * nd, "F6");
-      w.R6 = dalloc<float>(6 * nd, "R6");
-      w.Z6 = dalloc<float>(6 * nd, "Z6");
-      w.P6 = dalloc<float>(6 * nd, "P6");
-      w.AP6 = dalloc<float>(6 * nd, "AP6");
-      w.D6 = dalloc<float>(6 * nd, "D6");
+      const size_t n6 = (size_t)18 * mesh_.np;  // six right-hand sides, component-major
+      w.X6 = dalloc<double>(n6, "X6");
+      w.F6 = dalloc<double>(n6, "F6");
+      w.R6 = dalloc<float>(n6, "R6");
+      w.Z6 = dalloc<float>(n6, "Z6");
+      w.P6 = dalloc<float>(n6, "P6");
+      w.AP6 = dalloc<float>(n6, "AP6");
+      w.D6 = dalloc<float>(n6, "D6");
       w.cg6 = dalloc<Cg6State>(1, "cg6 state");
     }
     check(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), stream_), "ticket");
@@ -416,6 +438,7 @@ void Engine::ensure_slots(int n) {
     I.vals32 = w.vals32; I.kinv32 = w.kinv32; I.r32 = w.r32; I.z32 = w.z32; I.p32 = w.p32; I.Ap32 = w.Ap32;
     I.du32 = w.du32;
     I.X6 = w.X6; I.F6 = w.F6; I.R6 = w.R6; I.Z6 = w.Z6; I.P6 = w.P6; I.AP6 = w.AP6; I.D6 = w.D6; I.cg6 = w.cg6;
+    I.gpd = w.gpd;
     I.vars_old = nullptr;
     I.vars_new = w.vars_aux;
   }
@@ -430,7 +453,8 @@ void Engine::free_slots() {
   for (auto &w : slots_) {
     for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red, w.X6, w.F6})
       dfree(p);
-    for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6}) dfree(p);
+    for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6, w.gpd})
+      dfree(p);
     dfree(w.ticket);
     dfree(w.cg);
     dfree(w.cg6);
@@ -462,6 +486,13 @@ void Engine::download_out() {
   for (size_t s = 0; s < slots_.size(); ++s)
     check(cudaMemcpyAsync(&h_out_[s], slots_[s].out, sizeof(InstOut), cudaMemcpyDeviceToHost, stream_), "out");
   sync();
+}
+
+double Engine::listed_cg_its(const std::vector<int> &slots) {
+  download_out();
+  double its = 0.0;
+  for (int s : slots) its += h_out_[s].cg_its;
+  return its;
 }
 
 void Engine::sync() { check(cudaStreamSynchronize(stream_), "stream synchronize"); }
@@ -498,7 +529,7 @@ void Engine::timer_end(KernelTimer &t) {
 
 void Engine::set_kernel_timing(bool on) {
   sync();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_}) {
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_}) {
     t->enabled = on;
     t->used = 0;
     t->launches = 0;
@@ -513,6 +544,7 @@ bool Engine::kernel_stats(const std::string &family, long *launches, double *ms,
   else if (family == "assembly") t = &t_asm_;
   else if (family == "residual") t = &t_res_;
   else if (family == "spmv6") t = &t_spmv6_;
+  else if (family == "cg6_update") t = &t_upd6_;
   if (!t) return false;
   sync();
   for (size_t i = 0; i < t->used; ++i) {
@@ -558,26 +590,34 @@ void Engine::cg_solve(const std::vector<int> &slots) {
   check_launch(mgb_launch_cg_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg setup");
   // Algorithmic bytes per iteration and RVE (spmv): 81 values per row + x read + y written.
   const double nrow = (double)nndim();
-  const double spmv_bytes = (double)n * nrow * (81.0 * 8 + 2.0 * 8);
-  const double upd_bytes = (double)n * nrow * 8.0 * 8;
+  // Algorithmic bytes of one iteration of one instance.  SpMV: 81 values per row, x read, y written; update:
+  // read p, Ap, r, x, kinv, write x, r, z; p-update: read z, p, write p.  They are credited after the solve
+  // for the iterations each instance ran (an instance that has stopped skips the batch's later launches).
+  const double spmv_bytes = nrow * (81.0 * 8 + 2.0 * 8);
+  const double upd_bytes = nrow * 11.0 * 8;
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
     for (int it = 0; it < chunk; ++it) {
       if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-      timer_begin(t_spmv_, spmv_bytes);
+      timer_begin(t_spmv_, 0.0);
       launches_ += 3;
       check_launch(mgb_launch_cg_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg spmv");
       timer_end(t_spmv_);
-      timer_begin(t_update_, upd_bytes);
+      timer_begin(t_update_, 0.0);
       check_launch(mgb_launch_cg_update(&mesh_, d_insts_, d_list_, n, stream_), "cg update");
-      timer_end(t_update_);
       check_launch(mgb_launch_cg_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg p-update");
+      timer_end(t_update_);
     }
     done_its += chunk;
     check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
     sync();
     if (*h_count_ == 0) break;
+  }
+  if (t_spmv_.enabled) {
+    const double its = listed_cg_its(slots);
+    timer_add_bytes(t_spmv_, its * spmv_bytes);
+    timer_add_bytes(t_update_, its * upd_bytes);
   }
 }
 
@@ -595,27 +635,51 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   launches_ += 1;
   check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
   const double nrow = (double)nndim();
-  const double spmv_bytes = (double)n * nrow * (81.0 * 4 + 2.0 * 4);
-  const double upd_bytes = (double)n * nrow * 8.0 * 4;
+  // per iteration and instance, as in cg_solve; the symmetric half stores 42 values per row
+  const double spmv_bytes = nrow * ((sym32_ ? 42.0 : 81.0) * 4 + 2.0 * 4);
+  const double upd_bytes = nrow * 11.0 * 4;
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
     for (int it = 0; it < chunk; ++it) {
       if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-      timer_begin(t_spmv_, spmv_bytes);
+      timer_begin(t_spmv_, 0.0);
       launches_ += 3;
       check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg32 spmv");
       timer_end(t_spmv_);
-      timer_begin(t_update_, upd_bytes);
+      timer_begin(t_update_, 0.0);
       check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
-      timer_end(t_update_);
       check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
+      timer_end(t_update_);
     }
     done_its += chunk;
     check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
     sync();
     if (*h_count_ == 0) break;
   }
+  if (t_spmv_.enabled) {
+    const double its = listed_cg_its(slots);
+    timer_add_bytes(t_spmv_, its * spmv_bytes);
+    timer_add_bytes(t_update_, its * upd_bytes);
+  }
+}
+
+// Algorithmic bytes: the values written once; full stencil: u and the history read once per element;
+// symmetric half: the Gauss-point tangent terms (8 floats per Gauss point of a damage element) read once.
+void Engine::assemble32(int nlist) {
+  if (sym32_) {
+    timer_begin(t_asm_, (double)nlist * (4.0 * kSymSlots * 9 * mesh_.np + 4.0 * 64.0 * mesh_.nelem));
+    launches_ += 1;
+    check_launch(mgb_launch_assembly_sym32(&mesh_, &mats_, d_etype_, d_k0g32_, d_ke32_, d_dsh32_, d_insts_, d_list_,
+                                           nlist, stream_),
+                 "assembly (symmetric FP32)");
+  } else {
+    timer_begin(t_asm_, (double)nlist * (4.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
+    launches_ += 9;
+    check_launch(mgb_launch_assembly32(&mesh_, &mats_, d_etype_, d_dsh_, d_ke32_, d_insts_, d_list_, nlist, stream_),
+                 "assembly (FP32)");
+  }
+  timer_end(t_asm_);
 }
 
 // Implicit ctan of the listed slots at their current u with their vars_old: assemble the FP32 tangent, form
@@ -626,15 +690,14 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   std::vector<int> its(n, 0);
   upload_insts();
   upload_list(slots);
-  timer_begin(t_asm_, (double)n * (4.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
-  launches_ += 9;
-  check_launch(mgb_launch_assembly32(&mesh_, &mats_, d_etype_, d_dsh_, d_ke32_, d_insts_, d_list_, n, stream_),
-               "tangent assembly");
-  timer_end(t_asm_);
+  assemble32(n);
   launches_ += 1;
   check_launch(mgb_launch_t6_rhs(&mesh_, d_insts_, d_list_, n, stream_), "tangent rhs");
   const double nrow = (double)nndim();
-  const double spmv_bytes = (double)n * nrow * (81.0 * 4 + 2.0 * 6 * 4);
+  // Per iteration and instance: SpMV 81 values per row, 6 x read and 6 y written; update: read P, AP, R, D,
+  // write D, R, Z; p-update: read Z, P, write P (per right-hand side).  Credited per instance iteration.
+  const double spmv_bytes = nrow * ((sym32_ ? 42.0 : 81.0) * 4 + 2.0 * 6 * 4);
+  const double upd6_bytes = nrow * 6.0 * 10.0 * 4;
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   std::vector<int> live = slots;
   std::vector<int> live_idx(n);
@@ -682,12 +745,14 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
     while (done_its <= cg_max_its_) {
       for (int it = 0; it < chunk; ++it) {
         if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-        timer_begin(t_spmv6_, spmv_bytes * nl / n);
+        timer_begin(t_spmv6_, 0.0);
         launches_ += 3;
         check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 spmv");
         timer_end(t_spmv6_);
+        timer_begin(t_upd6_, 0.0);
         check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");
         check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
+        timer_end(t_upd6_);
       }
       done_its += chunk;
       check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
@@ -700,6 +765,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
     for (size_t a = 0; a < live.size(); ++a) {
       its[live_idx[a]] += h_out_[live[a]].cg6_its;
       total_cg_its_ += h_out_[live[a]].cg6_its;
+      timer_add_bytes(t_spmv6_, h_out_[live[a]].cg6_its * spmv_bytes);
+      timer_add_bytes(t_upd6_, h_out_[live[a]].cg6_its * upd6_bytes);
     }
   }
   upload_list(slots);
@@ -749,15 +816,15 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     if (active.empty()) break;
     upload_list(active);
     const int na = (int)active.size();
-    timer_begin(t_asm_, (double)na * ((mixed ? 4.0 : 8.0) * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
-    launches_ += 9;
-    if (mixed)
-      check_launch(mgb_launch_assembly32(&mesh_, &mats_, d_etype_, d_dsh_, d_ke32_, d_insts_, d_list_, na, stream_),
-                   "assembly");
-    else
+    if (mixed) {
+      assemble32(na);
+    } else {
+      timer_begin(t_asm_, (double)na * (8.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
+      launches_ += 9;
       check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, na, stream_),
                    "assembly");
-    timer_end(t_asm_);
+      timer_end(t_asm_);
+    }
     launches_ += 1;
     if (mixed) {
       // Inexact Newton: the FP64 residual corrects each FP32 solve, so a correction only needs to gain the

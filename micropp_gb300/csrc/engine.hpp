@@ -43,6 +43,7 @@ struct Slot {
         *du32 = nullptr;
   double *X6 = nullptr, *F6 = nullptr;
   float *R6 = nullptr, *Z6 = nullptr, *P6 = nullptr, *AP6 = nullptr, *D6 = nullptr;
+  float *gpd = nullptr;
   unsigned int *ticket = nullptr;
   CgState *cg = nullptr;
   Cg6State *cg6 = nullptr;
@@ -104,6 +105,7 @@ class Engine {
   bool kernel_stats(const std::string &family, long *launches, double *ms, double *bytes);
   long total_cg_its() const { return total_cg_its_; }
   long kernel_launches() const { return launches_; }
+  bool ell32_symmetric() const { return sym32_; }
   int mpi_rank() const { return mpi_rank_; }
 
  private:
@@ -112,6 +114,8 @@ class Engine {
   void build_elem_types(const micropp3_config &cfg);
   void build_materials(const micropp3_config &cfg);
   void build_phase_stiffness();
+  // FP32 Jacobian of the listed slots at their current u (the residual at that u was the last one made).
+  void assemble32(int nlist);
   void ensure_slots(int n);
   void free_slots();
   void calc_ctan_lin();
@@ -131,6 +135,12 @@ class Engine {
   void allocate_vars(GpState &g);
   void timer_begin(KernelTimer &t, double bytes);
   void timer_end(KernelTimer &t);
+  // Adds algorithmic bytes to a timer whose launches were recorded with 0 bytes.
+  void timer_add_bytes(KernelTimer &t, double bytes) {
+    if (t.enabled) t.pending_bytes += bytes;
+  }
+  // Sum of out.cg_its over the listed slots (reads the outputs back; call when timing is enabled).
+  double listed_cg_its(const std::vector<int> &slots);
   void sync();
 
   int ngp_ = 0;
@@ -149,6 +159,8 @@ class Engine {
   double bmat_[8][6][24];
   double dsh_[8 * 24];
   double ke_phase_[3][576];
+  std::vector<float> k0g32_;  // wg B_g^T C_phase B_g in FP32, [3][8][576]
+  bool sym32_ = false;        // the FP32 Jacobian is symmetric and stored as its upper half
   std::vector<int8_t> etype_;
   double Vm_ = 0, Vf_ = 0;
   double ctan_lin_[36] = {0};
@@ -158,7 +170,7 @@ class Engine {
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
-  float *d_ke32_ = nullptr;
+  float *d_ke32_ = nullptr, *d_k0g32_ = nullptr, *d_dsh32_ = nullptr;
   std::vector<Slot> slots_;
   std::vector<Inst> h_insts_;
   Inst *d_insts_ = nullptr;
@@ -169,7 +181,7 @@ class Engine {
   double last_ms_ = 0.0;
   long total_cg_its_ = 0;
   long launches_ = 0;  // kernels of this library launched by the handle
-  KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_;
+  KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_, t_upd6_;
 };
 
 }  // namespace mgb

@@ -127,7 +127,23 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, c
       const double *dg = &dsh[g * 24];
       double eps[6], s[6];
       gp_strain(dg, ue, eps);
-      law_stress(mat, eps, I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr, s);
+      const double *vg = I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr;
+      if (mat.type == 2 && I.gpd) {
+        // damage: the same stress as law_stress, plus the tangent terms for the FP32 Jacobian
+        double D, ta, tc;
+        law_damage_terms(mat, eps, vg, s, &D, &ta, &tc);
+        float *__restrict__ gpd = I.gpd;
+        const size_t st = (size_t)8 * m.nelem, o = (size_t)g * m.nelem + e;
+        gpd[o] = (float)ta;
+        gpd[st + o] = (float)tc;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) gpd[(2 + v) * st + o] = (float)s[v];
+        const double f = 1 - D;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) s[v] *= f;
+      } else {
+        law_stress(mat, eps, vg, s);
+      }
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
         const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
@@ -337,6 +353,162 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
   }
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Symmetric FP32 Jacobian by node gather (mixed form, every phase elastic or damage).
+//
+// Thread (node n, element position ep): of the 8 elements around n it takes the one at ep = dxq + 2 dyq +
+// 4 dzq, element (i-1+dxq, j-1+dyq, k-1+dzq), in which n is the local corner a = (1-dxq, 1-dyq, 1-dzq).  It
+// forms the 3x3 blocks of that element's matrix coupling a with every corner b at an upper slot of n:
+//   damage  (C_g = a_g C + c_g s_g s_g^T):  Ke_ab = sum_g a_g K0_g,ab + c_g wg (B_a,g^T s_g)(B_b,g^T s_g)^T
+//   elastic:                               Ke_ab = sum_g K0_g,ab
+// with K0_g = wg B_g^T C_phase B_g precomputed per phase and Gauss point, and (a_g, c_g, s_g) written by the
+// FP64 residual at the same displacement.  The 8 warps of a block (one element position each) add their
+// blocks into the block's 32 node rows in shared memory in a fixed order; the rows are then written once,
+// coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their full rows (the lower-slot
+// blocks of their interior neighbours are read from them).
+constexpr int kAsmNodes = 32;
+constexpr int kAsmRow = kSymSlots * 9 + 1;  // 127 floats: odd stride, conflict-free
+
+__host__ __device__ constexpr int corner_x(int b) { return ((b & 3) == 1 || (b & 3) == 2) ? 1 : 0; }
+__host__ __device__ constexpr int corner_y(int b) { return (b & 3) >= 2 ? 1 : 0; }
+__host__ __device__ constexpr int corner_z(int b) { return b >> 2; }
+__host__ __device__ constexpr int local_c(int ox, int oy, int oz) { return oz * 4 + (oy ? 3 - ox : ox); }
+// Upper-slot index (0..13) of the neighbour at offset (dx,dy,dz), or -1 for a lower slot.
+__host__ __device__ constexpr int sym_slot(int dx, int dy, int dz) {
+  return ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1) >= 13) ? (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1) - 13 : -1;
+}
+template <int A, int B>
+struct SymPair {
+  static constexpr int slot = sym_slot(corner_x(B) - corner_x(A), corner_y(B) - corner_y(A), corner_z(B) - corner_z(A));
+};
+
+template <int EP, int B>
+__device__ __forceinline__ void asm_add_b(float (&acc)[8][9], float A, float cw, const float (&va)[3],
+                                          const float *dg, const float (&s)[6], const float *__restrict__ K) {
+  constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
+  if constexpr (SymPair<a, B>::slot >= 0) {
+    const float gx = dg[B * 3], gy = dg[B * 3 + 1], gz = dg[B * 3 + 2];
+    const float vb[3] = {gx * s[0] + gy * s[3] + gz * s[4], gy * s[1] + gx * s[3] + gz * s[5],
+                         gz * s[2] + gx * s[4] + gy * s[5]};
+#pragma unroll
+    for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+      for (int fj = 0; fj < 3; ++fj)
+        acc[B][fi * 3 + fj] += A * __ldg(&K[(a * 3 + fi) * 24 + B * 3 + fj]) + cw * va[fi] * vb[fj];
+  }
+}
+
+template <int EP, int B>
+__device__ __forceinline__ void asm_add_b_elastic(float (&acc)[8][9], const float *__restrict__ K) {
+  constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
+  if constexpr (SymPair<a, B>::slot >= 0) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[B][q] += __ldg(&K[(a * 3 + q / 3) * 24 + B * 3 + q % 3]);
+  }
+}
+
+template <int EP>
+__device__ __forceinline__ void asm_sym_ep(const MeshDev &m, const Mats &mats, const int8_t *__restrict__ etype,
+                                           const float *__restrict__ k0g, const float *__restrict__ kesum,
+                                           const float *dsh, const float *__restrict__ gpd, int i, int j, int k,
+                                           float (&acc)[8][9]) {
+  constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
+  const int ex = i - 1 + (EP & 1), ey = j - 1 + ((EP >> 1) & 1), ez = k - 1 + (EP >> 2);
+  if (ex < 0 || ey < 0 || ez < 0 || ex >= m.nex || ey >= m.ney || ez >= m.nez) return;
+  const int e = (ez * m.ney + ey) * m.nex + ex;
+  const int ph = etype[e];
+  if (mats.m[ph].type == 0) {
+    const float *K = kesum + ph * 576;
+    asm_add_b_elastic<EP, 0>(acc, K); asm_add_b_elastic<EP, 1>(acc, K);
+    asm_add_b_elastic<EP, 2>(acc, K); asm_add_b_elastic<EP, 3>(acc, K);
+    asm_add_b_elastic<EP, 4>(acc, K); asm_add_b_elastic<EP, 5>(acc, K);
+    asm_add_b_elastic<EP, 6>(acc, K); asm_add_b_elastic<EP, 7>(acc, K);
+    return;
+  }
+  const size_t st = (size_t)8 * m.nelem;
+  const float wg = (float)m.wg;
+#pragma unroll 1
+  for (int g = 0; g < 8; ++g) {
+    const size_t o = (size_t)g * m.nelem + e;
+    const float A = __ldg(&gpd[o]), cw = __ldg(&gpd[st + o]) * wg;
+    float s[6];
+#pragma unroll
+    for (int v = 0; v < 6; ++v) s[v] = __ldg(&gpd[(2 + v) * st + o]);
+    const float *dg = dsh + g * 24;
+    const float gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+    const float va[3] = {gx * s[0] + gy * s[3] + gz * s[4], gy * s[1] + gx * s[3] + gz * s[5],
+                         gz * s[2] + gx * s[4] + gy * s[5]};
+    const float *K = k0g + ((size_t)ph * 8 + g) * 576;
+    asm_add_b<EP, 0>(acc, A, cw, va, dg, s, K); asm_add_b<EP, 1>(acc, A, cw, va, dg, s, K);
+    asm_add_b<EP, 2>(acc, A, cw, va, dg, s, K); asm_add_b<EP, 3>(acc, A, cw, va, dg, s, K);
+    asm_add_b<EP, 4>(acc, A, cw, va, dg, s, K); asm_add_b<EP, 5>(acc, A, cw, va, dg, s, K);
+    asm_add_b<EP, 6>(acc, A, cw, va, dg, s, K); asm_add_b<EP, 7>(acc, A, cw, va, dg, s, K);
+  }
+}
+
+template <int EP>
+__device__ __forceinline__ void asm_sym_store(const float (&acc)[8][9], float *row) {
+  constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const int sl = sym_slot(corner_x(b) - corner_x(a), corner_y(b) - corner_y(a), corner_z(b) - corner_z(a));
+    if (sl >= 0)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) row[sl * 9 + q] += acc[b][q];
+  }
+}
+
+#define MGB_EP_SWITCH(w, CALL) \
+  switch (w) {                 \
+    case 0: CALL(0); break;    \
+    case 1: CALL(1); break;    \
+    case 2: CALL(2); break;    \
+    case 3: CALL(3); break;    \
+    case 4: CALL(4); break;    \
+    case 5: CALL(5); break;    \
+    case 6: CALL(6); break;    \
+    default: CALL(7); break;   \
+  }
+
+__global__ void __launch_bounds__(kAsmNodes * 8) k_asm_sym32(MeshDev m, Mats mats, const int8_t *etype,
+                                                              const float *k0g, const float *kesum,
+                                                              const float *dsh_g, const Inst *insts,
+                                                              const int *list) {
+  __shared__ float rows[kAsmNodes * kAsmRow];
+  __shared__ float dsh[8 * 24];
+  for (int t = threadIdx.x; t < kAsmNodes * kAsmRow; t += blockDim.x) rows[t] = 0.f;
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
+  __syncthreads();
+  const Inst &I = insts[list[blockIdx.y]];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n = blockIdx.x * kAsmNodes + lane;
+  const bool valid = n < m.nn;
+  const int i = n % m.nx, j = (n / m.nx) % m.ny, k = n / m.nxny;
+  float acc[8][9];
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[b][q] = 0.f;
+  if (valid) {
+#define MGB_ASM_CALL(E) asm_sym_ep<E>(m, mats, etype, k0g, kesum, dsh, I.gpd, i, j, k, acc)
+    MGB_EP_SWITCH(w, MGB_ASM_CALL)
+#undef MGB_ASM_CALL
+  }
+  // element positions add into the node rows one after the other (fixed summation order)
+  for (int p = 0; p < 8; ++p) {
+    __syncthreads();
+    if (w == p && valid) {
+#define MGB_STORE_CALL(E) asm_sym_store<E>(acc, &rows[lane * kAsmRow])
+      MGB_EP_SWITCH(w, MGB_STORE_CALL)
+#undef MGB_STORE_CALL
+    }
+  }
+  __syncthreads();
+  float *__restrict__ vals = I.vals32;
+  const size_t np = m.np;
+  for (int E = w; E < kSymSlots * 9; E += 8) vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = rows[lane * kAsmRow + E];
+}
+
 // Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
 template <typename T>
 __global__ void k_zero_vals(size_t count, const Inst *insts, const int *list) {
@@ -480,6 +652,15 @@ int mgb_launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype,
 int mgb_launch_assembly32(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
                           const float *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   return launch_assembly<float>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
+}
+
+int mgb_launch_assembly_sym32(const MeshDev *m, const Mats *mats, const int8_t *etype, const float *k0g,
+                              const float *kesum, const float *dsh32, const Inst *insts, const int *list, int nlist,
+                              cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_asm_sym32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, 0, s>>>(*m, *mats, etype, k0g, kesum, dsh32,
+                                                                             insts, list);
+  return (int)cudaGetLastError();
 }
 
 int mgb_launch_elem_fields(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh, const double *u,

@@ -34,6 +34,11 @@ int mgb_launch_cg_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const i
 
 int mgb_launch_assembly32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                           const float *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// Symmetric FP32 Jacobian (every phase elastic or damage): k0g = wg B_g^T C B_g per phase and Gauss point
+// [3][8][576], kesum = its sum over g per phase [3][576], dsh32 = the shape-function gradients [8][24].
+int mgb_launch_assembly_sym32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *k0g,
+                              const float *kesum, const float *dsh32, const mgb::Inst *insts, const int *list,
+                              int nlist, cudaStream_t s);
 int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg32_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);

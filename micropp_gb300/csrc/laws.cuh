@@ -80,6 +80,26 @@ __device__ __forceinline__ bool law_damage(const MatDev &m, const double *eps, d
   return true;
 }
 
+// Damage law for the residual with the terms of its consistent tangent (the damage branch of law_ctan_exact):
+// s holds the undamaged stress C eps on return, the damaged stress is (1 - D) s, and
+// d sigma / d eps = a C + c s (x) s.
+__device__ __forceinline__ void law_damage_terms(const MatDev &m, const double *eps, const double *vars, double *s,
+                                                 double *D, double *a, double *c) {
+  const double r_old = vars ? vars[0] : 0.0;
+  const double D_old = vars ? vars[1] : 0.0;
+  double r;
+  const bool loading = law_damage(m, eps, r_old, D_old, &r, D, s);
+  if (!loading) {
+    *a = 1 - D_old;
+    *c = 0.0;
+    return;
+  }
+  const double q = law_damage_hardening(m, r);
+  const double qp = (r < m.dmg_r0) ? 0.0 : (r < m.dmg_r1 ? 10.0 : 5.0);
+  *a = q / r;
+  *c = (qp - *a) / (r * r);
+}
+
 // get_stress of the three laws (material.cpp:76-82, 149-162, 270-284).
 __device__ __forceinline__ void law_stress(const MatDev &m, const double *eps, const double *vars, double *s) {
   if (m.type == 0) {

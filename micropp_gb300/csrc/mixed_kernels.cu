@@ -68,15 +68,77 @@ __device__ __forceinline__ int nb_of(const MeshDev &m, int n, int s) {
   return n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
 }
 
+// The 3x3 block (row-major fi, fj) of FP32 ELL row n at stencil slot s, whose neighbour is nb, from either
+// storage: the full stencil, or the symmetric half, where a lower slot s is the transpose of slot 26 - s of
+// the neighbour's row.
+template <typename T>
+__device__ __forceinline__ void ell32_block(const MeshDev &m, const float *__restrict__ vals, int n, int nb, int s,
+                                            T (&K)[9]) {
+  const size_t np = m.np;
+  if (!m.sym32) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) K[q] = (T)vals[(size_t)(s * 9 + q) * np + n];
+  } else if (s >= 13) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) K[q] = (T)vals[(size_t)((s - 13) * 9 + q) * np + n];
+  } else {
+#pragma unroll
+    for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+      for (int fj = 0; fj < 3; ++fj) K[fi * 3 + fj] = (T)vals[(size_t)((13 - s) * 9 + fj * 3 + fi) * np + nb];
+  }
+}
+
+// Four consecutive floats starting R floats into the 8 loaded as lo, hi (R uniform over the grid).
+template <int R>
+__device__ __forceinline__ float4 shift4(const float4 lo, const float4 hi) {
+  if constexpr (R == 0) return lo;
+  else if constexpr (R == 1) return make_float4(lo.y, lo.z, lo.w, hi.x);
+  else if constexpr (R == 2) return make_float4(lo.z, lo.w, hi.x, hi.y);
+  else return make_float4(lo.w, hi.x, hi.y, hi.z);
+}
+
+// Lower-slot contribution of the symmetric FP32 ELL to 4 consecutive rows n0..n0+3: the rows' block at slot
+// sl is the transpose of block 13 - sl of rows a0 + R .. a0 + R + 3 (a0 = n0 + doff - R, 16-byte aligned),
+// read as two aligned 16-byte loads per entry.
+template <int R>
+__device__ __forceinline__ void lower4(const float *__restrict__ vt, size_t np, int a0, const float (&x)[6][3],
+                                       int dx, float (&y)[4][3]) {
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    const int fi = e / 3, fj = e % 3;
+    const float4 *row = reinterpret_cast<const float4 *>(vt + (size_t)(fj * 3 + fi) * np + a0);
+    const float4 t = shift4<R>(__ldg(row), __ldg(row + 1));
+    y[0][fi] = fmaf(t.x, x[0 + dx][fj], y[0][fi]);
+    y[1][fi] = fmaf(t.y, x[1 + dx][fj], y[1][fi]);
+    y[2][fi] = fmaf(t.z, x[2 + dx][fj], y[2][fi]);
+    y[3][fi] = fmaf(t.w, x[3 + dx][fj], y[3][fi]);
+  }
+}
+
+// Entry index of diagonal entry (d, d) of row n's own block in the FP32 ELL.
+__device__ __forceinline__ size_t ell32_diag(const MeshDev &m, int n, int d) {
+  return (size_t)((m.sym32 ? 0 : 13 * 9) + d * 3 + d) * m.np + n;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------------
 // Single right-hand side FP32 CG (the Newton correction of the mixed form).
+//
+// Dot products: each thread sums its few products in FP32, the grid reduction adds the thread sums in FP32
+// within a warp and in FP64 above (grid_sum_f).
+
+constexpr int kRowsPerThread = 4;   // vector kernels: rows per thread
+constexpr int kSpmvNodes = 4;       // FP32 SpMV: consecutive nodes per thread (one 16-byte load per entry)
+constexpr int kSpmvBlock = 128;
+constexpr int kSpmv6Nodes = 2;      // 6-RHS SpMV: consecutive nodes per thread (one 8-byte load per entry)
+constexpr int kSpmv6Block = 128;
 
 __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[2] = {0.0, 0.0};
+  float acc[2] = {0.f, 0.f};
   if (n < m.nn) {
     int i, j, k;
     const bool b = bnd(m, n, i, j, k);
@@ -90,7 +152,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int row = n * 3 + d;
-      const float kd = b ? 1.0f : 1.0f / vals[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+      const float kd = b ? 1.0f : 1.0f / vals[ell32_diag(m, n, d)];
       const float r = (float)bb[row];
       const float z = kd * r;
       kinv[row] = kd;
@@ -98,12 +160,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
       rv[row] = r;
       zv[row] = z;
       pv[row] = z;
-      acc[0] += (double)r * (double)z;
-      acc[1] += (double)z * (double)z;
+      acc[0] = fmaf(r, z, acc[0]);
+      acc[1] = fmaf(z, z, acc[1]);
     }
   }
   double tot[2];
-  if (grid_sum<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     CgState *c = I.cg;
     c->rz = tot[0];
     c->pnorm0 = sqrt(tot[1]);
@@ -118,55 +180,111 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
   }
 }
 
-__global__ void __launch_bounds__(kNodeBlock) k_cg32_spmv(MeshDev m, const Inst *insts, const int *list) {
+// Ap = K p for kSpmvNodes consecutive nodes per thread.  Each stored ELL entry of the group is one 16-byte
+// load (np is a multiple of 32 and the group starts at a multiple of 4), and the 6 neighbours a group row
+// needs along x are loaded once for the 3 x-slots.  Sym: the 13 lower slots are read transposed from the
+// neighbours' rows (scalar loads, mostly L2 hits: those rows are streamed by nearby blocks).  A boundary node
+// of the group is an identity row: its stencil sum (over clamped neighbour indices) is discarded.
+template <bool Sym>
+__global__ void __launch_bounds__(kSpmvBlock) k_cg32_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg->done) return;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[1] = {0.0};
-  if (n < m.nn) {
-    int i, j, k;
+  const int n0 = (blockIdx.x * blockDim.x + threadIdx.x) * kSpmvNodes;
+  float acc[1] = {0.f};
+  if (n0 < m.nn) {
     const float *__restrict__ p = I.p32;
     float *__restrict__ Ap = I.Ap32;
-    if (bnd(m, n, i, j, k)) {
+    bool bn[kSpmvNodes];
+    bool any_interior = false;
+#pragma unroll
+    for (int q = 0; q < kSpmvNodes; ++q) {
+      int i, j, k;
+      bn[q] = (n0 + q >= m.nn) || bnd(m, n0 + q, i, j, k);
+      any_interior |= !bn[q];
+    }
+    float y[kSpmvNodes][3];
+#pragma unroll
+    for (int q = 0; q < kSpmvNodes; ++q) y[q][0] = y[q][1] = y[q][2] = 0.f;
+    if (any_interior) {
+      const size_t np = m.np, np4 = np / 4;
+      const float *__restrict__ vals = I.vals32;
+      const float4 *__restrict__ v4 = reinterpret_cast<const float4 *>(vals + n0);
+      const int last = m.nn - 1;
+#pragma unroll 1
+      for (int zy = 0; zy < 9; ++zy) {
+        const int base = n0 + (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx - 1;
+        float x[kSpmvNodes + 2][3];
+        int nbw[kSpmvNodes + 2];
+#pragma unroll
+        for (int w = 0; w < kSpmvNodes + 2; ++w) {
+          const int nb = min(max(base + w, 0), last);
+          nbw[w] = nb;
+          x[w][0] = p[nb * 3 + 0];
+          x[w][1] = p[nb * 3 + 1];
+          x[w][2] = p[nb * 3 + 2];
+        }
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const int sl = zy * 3 + dx;
+          if (!Sym || sl >= 13) {
+            const float4 *vs = v4 + (size_t)((Sym ? sl - 13 : sl) * 9) * np4;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) {
+              const float4 a = Sym ? __ldg(vs + e * np4) : __ldcs(vs + e * np4);
+              const int fi = e / 3, fj = e % 3;
+              y[0][fi] = fmaf(a.x, x[0 + dx][fj], y[0][fi]);
+              y[1][fi] = fmaf(a.y, x[1 + dx][fj], y[1][fi]);
+              y[2][fi] = fmaf(a.z, x[2 + dx][fj], y[2][fi]);
+              y[3][fi] = fmaf(a.w, x[3 + dx][fj], y[3][fi]);
+            }
+          } else {
+            // lower slot: rows n0 + doff + q hold the transposed blocks; doff & 3 is the same for every group
+            const float *vt = vals + (size_t)((13 - sl) * 9) * np;
+            const int doff = (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx + (dx - 1);
+            const int r = doff & 3, a0 = n0 + doff - r;
+            if (a0 >= 0 && a0 + 8 <= m.np) {
+              if (r == 0) lower4<0>(vt, np, a0, x, dx, y);
+              else if (r == 1) lower4<1>(vt, np, a0, x, dx, y);
+              else if (r == 2) lower4<2>(vt, np, a0, x, dx, y);
+              else lower4<3>(vt, np, a0, x, dx, y);
+            } else {  // first or last groups of the array: clamped scalar loads
+#pragma unroll
+              for (int q = 0; q < kSpmvNodes; ++q) {
+                const float *vq = vt + nbw[q + dx];
+#pragma unroll
+                for (int e = 0; e < 9; ++e) {
+                  const int fi = e / 3, fj = e % 3;  // block (fi, fj) of row n0+q = entry (fj, fi) of the neighbour
+                  y[q][fi] = fmaf(__ldg(vq + (size_t)(fj * 3 + fi) * np), x[q + dx][fj], y[q][fi]);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kSpmvNodes; ++q) {
+      const int n = n0 + q;
+      if (n >= m.nn) break;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const float pv = p[n * 3 + d];
-        Ap[n * 3 + d] = pv;
-        acc[0] += (double)pv * (double)pv;
+        const float yv = bn[q] ? pv : y[q][d];
+        Ap[n * 3 + d] = yv;
+        acc[0] = fmaf(pv, yv, acc[0]);
       }
-    } else {
-      const float *__restrict__ v = I.vals32 + n;
-      const size_t np = m.np;
-      float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-#pragma unroll
-      for (int s = 0; s < 27; ++s) {
-        const int nb = nb_of(m, n, s);
-        const float x0 = p[nb * 3 + 0], x1 = p[nb * 3 + 1], x2 = p[nb * 3 + 2];
-        const float *vs = v + (size_t)(s * 9) * np;
-        y0 = fmaf(__ldcs(vs + 0 * np), x0, y0);
-        y0 = fmaf(__ldcs(vs + 1 * np), x1, y0);
-        y0 = fmaf(__ldcs(vs + 2 * np), x2, y0);
-        y1 = fmaf(__ldcs(vs + 3 * np), x0, y1);
-        y1 = fmaf(__ldcs(vs + 4 * np), x1, y1);
-        y1 = fmaf(__ldcs(vs + 5 * np), x2, y1);
-        y2 = fmaf(__ldcs(vs + 6 * np), x0, y2);
-        y2 = fmaf(__ldcs(vs + 7 * np), x1, y2);
-        y2 = fmaf(__ldcs(vs + 8 * np), x2, y2);
-      }
-      Ap[n * 3 + 0] = y0;
-      Ap[n * 3 + 1] = y1;
-      Ap[n * 3 + 2] = y2;
-      acc[0] = (double)(p[n * 3 + 0] * y0 + p[n * 3 + 1] * y1 + p[n * 3 + 2] * y2);
     }
   }
   double tot[1];
-  if (grid_sum<1>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<1>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     CgState *c = I.cg;
     c->pAp = tot[0];
     c->alpha = c->rz / tot[0];
   }
 }
 
+// du += alpha p; r -= alpha Ap; z = kinv r, kRowsPerThread rows per thread (loads of all rows first); the
+// last block sets beta, the norms and the stop flag.
 __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const CgState *cs = I.cg;
@@ -179,18 +297,33 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Ins
   const float *__restrict__ p = I.p32;
   const float *__restrict__ Ap = I.Ap32;
   const float *__restrict__ kinv = I.kinv32;
-  double acc[2] = {0.0, 0.0};
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x) {
-    du[row] = fmaf(alpha, p[row], du[row]);
-    const float r = fmaf(-alpha, Ap[row], rv[row]);
-    const float z = kinv[row] * r;
-    rv[row] = r;
-    zv[row] = z;
-    acc[0] += (double)(z * z);
-    acc[1] += (double)(r * z);
+  const int stride = gridDim.x * blockDim.x;
+  float acc[2] = {0.f, 0.f};
+  for (int row0 = blockIdx.x * blockDim.x + threadIdx.x; row0 < nrow; row0 += kRowsPerThread * stride) {
+    float pv[kRowsPerThread], av[kRowsPerThread], rr[kRowsPerThread], dv[kRowsPerThread], kv[kRowsPerThread];
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) {
+        pv[q] = p[row]; av[q] = Ap[row]; rr[q] = rv[row]; dv[q] = du[row]; kv[q] = kinv[row];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) {
+        du[row] = fmaf(alpha, pv[q], dv[q]);
+        const float r = fmaf(-alpha, av[q], rr[q]);
+        const float z = kv[q] * r;
+        rv[row] = r;
+        zv[row] = z;
+        acc[0] = fmaf(z, z, acc[0]);
+        acc[1] = fmaf(r, z, acc[1]);
+      }
+    }
   }
   double tot[2];
-  if (grid_sum<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     CgState *c = I.cg;
     c->pnorm = sqrt(tot[0]);
     c->beta = tot[1] / c->rz;
@@ -217,8 +350,23 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_pupdate(MeshDev m, const In
   const int nrow = m.nn * 3;
   float *__restrict__ p = I.p32;
   const float *__restrict__ z = I.z32;
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += gridDim.x * blockDim.x)
-    p[row] = fmaf(beta, p[row], z[row]);
+  const int stride = gridDim.x * blockDim.x;
+  for (int row0 = blockIdx.x * blockDim.x + threadIdx.x; row0 < nrow; row0 += kRowsPerThread * stride) {
+    float pv[kRowsPerThread], zv[kRowsPerThread];
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) {
+        pv[q] = p[row];
+        zv[q] = z[row];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int row = row0 + q * stride;
+      if (row < nrow) p[row] = fmaf(beta, pv[q], zv[q]);
+    }
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
 
@@ -230,7 +378,7 @@ __global__ void k_add_du32(int nndim, const Inst *insts, const int *list) {
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Six right-hand sides of the implicit ctan.
+// Six right-hand sides of the implicit ctan.  The vectors are component-major, V[c6(i, d, np) + n].
 
 // f_i = -K_IB w_i on interior rows (FP64 accumulation of the FP32 tangent), 0 on boundary rows; x_i = 0.
 __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *insts, const int *list) {
@@ -239,12 +387,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
   double acc[6] = {0, 0, 0, 0, 0, 0};
   if (n < m.nn) {
     int i, j, k;
+    const bool b = bnd(m, n, i, j, k);
+    const size_t np = m.np;
     double f[6][3];
 #pragma unroll
     for (int r = 0; r < 6; ++r) f[r][0] = f[r][1] = f[r][2] = 0.0;
-    if (!bnd(m, n, i, j, k)) {
-      const float *__restrict__ v = I.vals32 + n;
-      const size_t np = m.np;
+    if (!b) {
 #pragma unroll 1
       for (int s = 0; s < 27; ++s) {
         const int nb = nb_of(m, n, s);
@@ -253,8 +401,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
         double c[3];
         bc_coords(m, bi, bj, bk, c);
         double Kb[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) Kb[q] = (double)v[(size_t)(s * 9 + q) * np];
+        ell32_block(m, I.vals32, n, nb, s, Kb);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           double w[3];
@@ -270,17 +417,16 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const size_t idx = ((size_t)n * 6 + r) * 3 + d;
+        const size_t idx = c6(r, d, np) + n;
         F6[idx] = f[r][d];
         X6[idx] = 0.0;
         acc[r] += f[r][d] * f[r][d];
       }
     // Jacobi inverse of the tangent for the 6-RHS CG (boundary rows are identity rows)
     float *__restrict__ kinv = I.kinv32;
-    const bool b = bnd(m, n, i, j, k);
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-      kinv[n * 3 + d] = b ? 1.0f : 1.0f / I.vals32[(size_t)(13 * 9 + d * 3 + d) * m.np + n];
+      kinv[n * 3 + d] = b ? 1.0f : 1.0f / I.vals32[ell32_diag(m, n, d)];
   }
   double tot[6];
   if (grid_sum<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
@@ -298,27 +444,25 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
   if (n < m.nn) {
     int i, j, k;
     const bool b = bnd(m, n, i, j, k);
+    const size_t np = m.np;
+    const double *__restrict__ X6 = I.X6;
     double rf[6][3];
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-      for (int d = 0; d < 3; ++d) rf[r][d] = b ? 0.0 : I.F6[((size_t)n * 6 + r) * 3 + d];
+      for (int d = 0; d < 3; ++d) rf[r][d] = b ? 0.0 : I.F6[c6(r, d, np) + n];
     float kd[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) kd[d] = I.kinv32[n * 3 + d];
     if (!b) {
-      const float *__restrict__ v = I.vals32 + n;
-      const size_t np = m.np;
 #pragma unroll 1
       for (int s = 0; s < 27; ++s) {
         const int nb = nb_of(m, n, s);
         double Kb[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) Kb[q] = (double)v[(size_t)(s * 9 + q) * np];
-        const double *x = I.X6 + (size_t)nb * 18;
+        ell32_block(m, I.vals32, n, nb, s, Kb);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
-          const double x0 = x[r * 3], x1 = x[r * 3 + 1], x2 = x[r * 3 + 2];
+          const double x0 = X6[c6(r, 0, np) + nb], x1 = X6[c6(r, 1, np) + nb], x2 = X6[c6(r, 2, np) + nb];
 #pragma unroll
           for (int fi = 0; fi < 3; ++fi) rf[r][fi] -= Kb[fi * 3] * x0 + Kb[fi * 3 + 1] * x1 + Kb[fi * 3 + 2] * x2;
         }
@@ -332,7 +476,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const size_t idx = ((size_t)n * 6 + r) * 3 + d;
+        const size_t idx = c6(r, d, np) + n;
         const float rr = (float)rf[r][d];
         const float z = kd[d] * rr;
         R6[idx] = rr;
@@ -365,78 +509,134 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
   }
 }
 
-// AP = K P for the six right-hand sides, one pass over K; the last block sets alpha_r.
-__global__ void __launch_bounds__(kNodeBlock) k_cg6_spmv(MeshDev m, const Inst *insts, const int *list) {
+// AP = K P for the six right-hand sides, one pass over K for all six; kSpmv6Nodes consecutive nodes per
+// thread, so each stored ELL entry of the pair is one 8-byte load and the 4 neighbours a pair row needs
+// along x are loaded once for the 3 x-slots (Sym: lower slots transposed from the neighbours' rows, as in
+// k_cg32_spmv).  The last block sets alpha_i.
+template <bool Sym>
+__global__ void __launch_bounds__(kSpmv6Block) k_cg6_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg6->all_done) return;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  if (n < m.nn) {
-    int i, j, k;
+  const int n0 = (blockIdx.x * blockDim.x + threadIdx.x) * kSpmv6Nodes;
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (n0 < m.nn) {
+    const size_t np = m.np;
     const float *__restrict__ P = I.P6;
-    float y[18];
-    if (bnd(m, n, i, j, k)) {
+    float *__restrict__ AP = I.AP6;
+    bool bn[kSpmv6Nodes];
+    bool any_interior = false;
 #pragma unroll
-      for (int q = 0; q < 18; ++q) y[q] = P[(size_t)n * 18 + q];
-    } else {
+    for (int q = 0; q < kSpmv6Nodes; ++q) {
+      int i, j, k;
+      bn[q] = (n0 + q >= m.nn) || bnd(m, n0 + q, i, j, k);
+      any_interior |= !bn[q];
+    }
+    float y[kSpmv6Nodes][18];
 #pragma unroll
-      for (int q = 0; q < 18; ++q) y[q] = 0.f;
-      const float *__restrict__ v = I.vals32 + n;
-      const size_t np = m.np;
-#pragma unroll 3
-      for (int s = 0; s < 27; ++s) {
-        const int nb = nb_of(m, n, s);
-        float Kb[9];
+    for (int q = 0; q < kSpmv6Nodes; ++q)
 #pragma unroll
-        for (int q = 0; q < 9; ++q) Kb[q] = __ldcs(v + (size_t)(s * 9 + q) * np);
-        const float2 *x2 = reinterpret_cast<const float2 *>(P + (size_t)nb * 18);
-        float x[18];
+      for (int c = 0; c < 18; ++c) y[q][c] = 0.f;
+    if (any_interior) {
+      const size_t np2 = np / 2;
+      const float2 *__restrict__ v2 = reinterpret_cast<const float2 *>(I.vals32 + n0);
+      const int last = m.nn - 1;
+#pragma unroll 1
+      for (int zy = 0; zy < 9; ++zy) {
+        const int base = n0 + (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx - 1;
+        int nb[kSpmv6Nodes + 2];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          const float2 t = x2[q];
-          x[2 * q] = t.x;
-          x[2 * q + 1] = t.y;
+        for (int w = 0; w < kSpmv6Nodes + 2; ++w) nb[w] = min(max(base + w, 0), last);
+        float2 a[3][9];
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const int sl = zy * 3 + dx;
+          if (!Sym) {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[dx][e] = __ldcs(v2 + (size_t)(sl * 9 + e) * np2);
+          } else if (sl >= 13) {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[dx][e] = __ldg(v2 + (size_t)((sl - 13) * 9 + e) * np2);
+          } else {
+            // lower slot: rows n0 + doff + q (q = 0, 1) hold the transposed blocks; doff & 1 is uniform
+            const float *vt = I.vals32 + (size_t)((13 - sl) * 9) * np;
+            const int doff = (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx + (dx - 1);
+            const int r = doff & 1, a0 = n0 + doff - r;
+            if (a0 >= 0 && a0 + 4 <= m.np) {
+#pragma unroll
+              for (int e = 0; e < 9; ++e) {
+                const int fi = e / 3, fj = e % 3;
+                const float2 *row = reinterpret_cast<const float2 *>(vt + (size_t)(fj * 3 + fi) * np + a0);
+                const float2 lo = __ldg(row), hi = __ldg(row + 1);
+                a[dx][e] = r ? make_float2(lo.y, hi.x) : lo;
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < 9; ++e) {
+                const int fi = e / 3, fj = e % 3;
+                a[dx][e].x = __ldg(vt + (size_t)(fj * 3 + fi) * np + nb[0 + dx]);
+                a[dx][e].y = __ldg(vt + (size_t)(fj * 3 + fi) * np + nb[1 + dx]);
+              }
+            }
+          }
         }
 #pragma unroll
-        for (int r = 0; r < 6; ++r)
+        for (int r = 0; r < 6; ++r) {
+          float x[kSpmv6Nodes + 2][3];
 #pragma unroll
-          for (int fi = 0; fi < 3; ++fi) {
-            float a = y[r * 3 + fi];
-            a = fmaf(Kb[fi * 3 + 0], x[r * 3 + 0], a);
-            a = fmaf(Kb[fi * 3 + 1], x[r * 3 + 1], a);
-            a = fmaf(Kb[fi * 3 + 2], x[r * 3 + 2], a);
-            y[r * 3 + fi] = a;
-          }
+          for (int w = 0; w < kSpmv6Nodes + 2; ++w)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) x[w][d] = P[c6(r, d, np) + nb[w]];
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int e = 0; e < 9; ++e) {
+              const int fi = e / 3, fj = e % 3;
+              y[0][r * 3 + fi] = fmaf(a[dx][e].x, x[0 + dx][fj], y[0][r * 3 + fi]);
+              y[1][r * 3 + fi] = fmaf(a[dx][e].y, x[1 + dx][fj], y[1][r * 3 + fi]);
+            }
+        }
       }
     }
-    float2 *__restrict__ ap2 = reinterpret_cast<float2 *>(I.AP6 + (size_t)n * 18);
-    const float2 *p2 = reinterpret_cast<const float2 *>(P + (size_t)n * 18);
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      ap2[q] = make_float2(y[2 * q], y[2 * q + 1]);
-      const float2 pv = p2[q];
-      acc[(2 * q) / 3] += (double)(pv.x * y[2 * q]);
-      acc[(2 * q + 1) / 3] += (double)(pv.y * y[2 * q + 1]);
+    for (int q = 0; q < kSpmv6Nodes; ++q) {
+      const int n = n0 + q;
+      if (n >= m.nn) break;
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const size_t idx = c6(r, d, np) + n;
+          const float pv = P[idx];
+          const float yv = bn[q] ? pv : y[q][r * 3 + d];
+          AP[idx] = yv;
+          acc[r] = fmaf(pv, yv, acc[r]);
+        }
     }
   }
   double tot[6];
-  if (grid_sum<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     Cg6State *c = I.cg6;
     for (int r = 0; r < 6; ++r) c->alpha[r] = c->done[r] ? 0.0 : c->rz[r] / tot[r];
   }
 }
 
-// D += alpha P; R -= alpha AP; Z = kinv R per right-hand side; the last block sets beta_r and the stop flags.
+// D += alpha P; R -= alpha AP; Z = kinv R for the right-hand sides still iterating, one thread per node
+// (grid-stride); the last block sets beta_i and the stop flags.
 __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const Cg6State *cs = I.cg6;
   if (cs->all_done) return;
   float alpha[6];
+  bool live[6];
 #pragma unroll
-  for (int r = 0; r < 6; ++r) alpha[r] = (float)cs->alpha[r];
-  double acc[12];
+  for (int r = 0; r < 6; ++r) {
+    alpha[r] = (float)cs->alpha[r];
+    live[r] = !cs->done[r];
+  }
+  float acc[12];
 #pragma unroll
-  for (int q = 0; q < 12; ++q) acc[q] = 0.0;  // [0,6): z.z  [6,12): r.z
+  for (int q = 0; q < 12; ++q) acc[q] = 0.f;  // [0,6): z.z  [6,12): r.z
+  const size_t np = m.np;
   float *__restrict__ D6 = I.D6;
   float *__restrict__ R6 = I.R6;
   float *__restrict__ Z6 = I.Z6;
@@ -448,21 +648,29 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
 #pragma unroll
     for (int d = 0; d < 3; ++d) kd[d] = kinv[n * 3 + d];
 #pragma unroll
-    for (int r = 0; r < 6; ++r)
+    for (int r = 0; r < 6; ++r) {
+      if (!live[r]) continue;
+      float pv[3], av[3], rv[3], dv[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const size_t idx = ((size_t)n * 6 + r) * 3 + d;
-        D6[idx] = fmaf(alpha[r], P6[idx], D6[idx]);
-        const float rr = fmaf(-alpha[r], AP6[idx], R6[idx]);
+        const size_t idx = c6(r, d, np) + n;
+        pv[d] = P6[idx]; av[d] = AP6[idx]; rv[d] = R6[idx]; dv[d] = D6[idx];
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const size_t idx = c6(r, d, np) + n;
+        D6[idx] = fmaf(alpha[r], pv[d], dv[d]);
+        const float rr = fmaf(-alpha[r], av[d], rv[d]);
         const float z = kd[d] * rr;
         R6[idx] = rr;
         Z6[idx] = z;
-        acc[r] += (double)(z * z);
-        acc[6 + r] += (double)(rr * z);
+        acc[r] = fmaf(z, z, acc[r]);
+        acc[6 + r] = fmaf(rr, z, acc[6 + r]);
       }
+    }
   }
   double tot[12];
-  if (grid_sum<12>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<12>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     Cg6State *c = I.cg6;
     c->its += 1;
     int all = 1;
@@ -493,30 +701,33 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_pupdate(MeshDev m, const Ins
     beta[r] = (float)cs->beta[r];
     live[r] = !cs->done[r];
   }
+  const size_t np = m.np;
   float *__restrict__ P6 = I.P6;
   const float *__restrict__ Z6 = I.Z6;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x) {
+    float pv[18], zv[18];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      if (!live[r]) continue;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const size_t idx = ((size_t)n * 6 + r) * 3 + d;
-        P6[idx] = fmaf(beta[r], P6[idx], Z6[idx]);
+    for (int c = 0; c < 18; ++c)
+      if (live[c / 3]) {
+        pv[c] = P6[(size_t)c * np + n];
+        zv[c] = Z6[(size_t)c * np + n];
       }
-    }
+#pragma unroll
+    for (int c = 0; c < 18; ++c)
+      if (live[c / 3]) P6[(size_t)c * np + n] = fmaf(beta[c / 3], pv[c], zv[c]);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
 
-// X += D (FP64 accumulation of the FP32 correction).
+// X += D (FP64 accumulation of the FP32 correction), one thread per node.
 __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
-  const size_t total = (size_t)m.nn * 18;
+  const size_t np = m.np;
   double *__restrict__ X6 = I.X6;
   const float *__restrict__ D6 = I.D6;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
-    X6[t] += (double)D6[t];
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 18; ++c) X6[(size_t)c * np + n] += (double)D6[(size_t)c * np + n];
 }
 
 // ctan[v][i] = (1/V) sum over Gauss points of wg (C_gp B (w_i + x_i))_v, one thread per Gauss point, FP64.
@@ -534,6 +745,7 @@ __global__ void __launch_bounds__(128) k_ctan_avg(MeshDev m, Mats mats, const in
     const int e = t >> 3, g = t & 7;
     const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
     const int n0 = ez * m.nxny + ey * m.nx + ex;
+    const size_t np = m.np;
     const double *dg = &dsh[g * 24];
     const MatDev &mat = mats.m[etype[e]];
     int nodes[8];
@@ -569,8 +781,8 @@ __global__ void __launch_bounds__(128) k_ctan_avg(MeshDev m, Mats mats, const in
       double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
-        const double *x = I.X6 + ((size_t)nodes[a] * 6 + r) * 3;
-        double ux = x[0], uy = x[1], uz = x[2];
+        double ux = I.X6[c6(r, 0, np) + nodes[a]], uy = I.X6[c6(r, 1, np) + nodes[a]],
+               uz = I.X6[c6(r, 2, np) + nodes[a]];
         if (nb_bnd[a]) {
           double w[3];
           lift(cc[a], r, w);
@@ -621,21 +833,26 @@ int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, 
 
 int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_spmv<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  const dim3 g(cdiv(cdiv(m->nn, kSpmvNodes), kSpmvBlock), nlist);
+  if (m->sym32)
+    k_cg32_spmv<true><<<g, kSpmvBlock, 0, s>>>(*m, insts, list);
+  else
+    k_cg32_spmv<false><<<g, kSpmvBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg32_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_update<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  const unsigned g = cdiv((size_t)m->nn * 3, (size_t)kRowsPerThread * kNodeBlock);
+  k_cg32_update<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg32_pupdate(const MeshDev *m, const Inst *insts, const int *list, int nlist,
                             unsigned int *active_count, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_pupdate<<<dim3(cdiv((size_t)m->nn * 3, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list,
-                                                                                           active_count);
+  const unsigned g = cdiv((size_t)m->nn * 3, (size_t)kRowsPerThread * kNodeBlock);
+  k_cg32_pupdate<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
   return (int)cudaGetLastError();
 }
 
@@ -660,26 +877,30 @@ int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list,
 
 int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_spmv<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  const dim3 g(cdiv(cdiv(m->nn, kSpmv6Nodes), kSpmv6Block), nlist);
+  if (m->sym32)
+    k_cg6_spmv<true><<<g, kSpmv6Block, 0, s>>>(*m, insts, list);
+  else
+    k_cg6_spmv<false><<<g, kSpmv6Block, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_update<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg6_update<<<dim3(cdiv(m->nn, 2 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_pupdate(const MeshDev *m, const Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_pupdate<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
+  k_cg6_pupdate<<<dim3(cdiv(m->nn, 2 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_t6_accumulate(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_accumulate<<<dim3(cdiv((size_t)m->nn * 18, kNodeBlock * 8), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_t6_accumulate<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 

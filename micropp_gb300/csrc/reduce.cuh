@@ -1,9 +1,15 @@
-// reduce.cuh -- deterministic block and grid reductions (FP64).
+// reduce.cuh -- deterministic block and grid reductions.
 //
 // A grid reduction is "last block done": every block reduces its K values with warp shuffles, writes them
 // to its own slot of a partials array, fences, and takes a ticket; the block that draws the last ticket sums
 // all partials in a fixed order and publishes the result.  The result is bitwise reproducible from run to
 // run, and no kernel ever waits on another block.
+//
+// Two entry precisions: grid_sum takes FP64 per-thread values; grid_sum_f takes FP32 per-thread partials
+// (a thread's sum over its few rows), adds them in FP32 across the 32 lanes of a warp and in FP64 from the
+// warp sums up.  The FP64 pipe of the GPU runs at 1/64 of the FP32 rate, so FP64 per-row accumulation and
+// FP64 shuffles cost more than the memory traffic of a vector update; grid_sum_f keeps FP64 for the part of
+// the sum that has many terms.
 #pragma once
 
 #include "device.cuh"
@@ -12,6 +18,14 @@ namespace mgb {
 
 template <int K>
 __device__ __forceinline__ void warp_sum(double (&v)[K]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+}
+
+template <int K>
+__device__ __forceinline__ void warp_sum(float (&v)[K]) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -35,14 +49,33 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sh) {
   }
 }
 
-// Grid reduction over the blocks of one instance (blockIdx.x = 0..nblocks-1).  Returns true in the last
-// block, where `total` (valid in every thread of that block) holds the sum.
+// Block sum of FP32 per-thread partials: FP32 within each warp, FP64 across the warps.  The FP64 result is
+// valid in thread 0.  `sh` holds 32*K doubles.
 template <int K>
-__device__ __forceinline__ bool grid_sum(double (&v)[K], double *red, unsigned int *ticket, int nblocks,
-                                         double (&total)[K]) {
-  __shared__ double sh[32 * K];
+__device__ __forceinline__ void block_sum_f(float (&v)[K], double (&out)[K], double *sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  warp_sum<K>(v);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[wid * K + k] = (double)v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double a = sh[k];
+      for (int w = 1; w < nw; ++w) a += sh[w * K + k];
+      out[k] = a;
+    }
+  }
+}
+
+// Second half of a grid reduction: `v` holds the block's sums in thread 0.  Returns true in the last block,
+// where `total` (valid in every thread of that block) holds the sum over the blocks of the instance.
+template <int K>
+__device__ __forceinline__ bool grid_finish(const double (&v)[K], double *sh, double *red, unsigned int *ticket,
+                                            int nblocks, double (&total)[K]) {
   __shared__ bool last;
-  block_sum<K>(v, sh);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) red[(size_t)blockIdx.x * kRedStride + k] = v[k];
@@ -70,6 +103,26 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double *red, unsigned i
 #pragma unroll
   for (int k = 0; k < K; ++k) total[k] = res[k];
   return true;
+}
+
+// Grid reduction over the blocks of one instance (blockIdx.x = 0..nblocks-1) of FP64 per-thread values.
+template <int K>
+__device__ __forceinline__ bool grid_sum(double (&v)[K], double *red, unsigned int *ticket, int nblocks,
+                                         double (&total)[K]) {
+  __shared__ double sh[32 * K];
+  block_sum<K>(v, sh);
+  return grid_finish<K>(v, sh, red, ticket, nblocks, total);
+}
+
+// Grid reduction of FP32 per-thread partials (FP32 within a warp, FP64 above).
+template <int K>
+__device__ __forceinline__ bool grid_sum_f(float (&v)[K], double *red, unsigned int *ticket, int nblocks,
+                                           double (&total)[K]) {
+  __shared__ double sh[32 * K];
+  double bs[K];
+  block_sum_f<K>(v, bs, sh);
+  __syncthreads();  // sh is reused by the last block
+  return grid_finish<K>(bs, sh, red, ticket, nblocks, total);
 }
 
 }  // namespace mgb

@@ -33,7 +33,8 @@ import bench
 dist.init_process_group("gloo")
 rank = dist.get_rank()
 v = bench.max_over_ranks(dist, float(rank + 1) * 2.5, dist.get_world_size())
-print(json.dumps({{"rank": rank, "max": v}}))
+with open(os.path.join({out!r}, f"rank{{rank}}.json"), "w") as f:
+    json.dump({{"rank": rank, "max": v}}, f)
 dist.destroy_process_group()
 """
 
@@ -41,10 +42,11 @@ dist.destroy_process_group()
 def test_max_over_ranks_gloo(tmp_path):
     pytest.importorskip("torch")
     w = tmp_path / "w.py"
-    w.write_text(WORKER.format(root=ROOT))
+    w.write_text(WORKER.format(root=ROOT, out=str(tmp_path)))
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2", "--master-addr",
            "127.0.0.1", "--master-port", "29612", str(w)]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
-    vals = [json.loads(l)["max"] for l in r.stdout.splitlines() if l.startswith("{")]
+    # each rank writes its own file: two processes printing to one pipe may interleave their lines
+    vals = [json.load(open(tmp_path / f"rank{k}.json"))["max"] for k in range(2)]
     assert vals == [5.0, 5.0]
