@@ -260,11 +260,9 @@ def run_reference(args):
     }))
 
 
-def load_traffic(n, family="spmv", fp32=False, sym=False):
+def load_traffic(n, family="spmv", fp32=False):
     """DRAM bytes of one RVE's launch of the kernel from a committed ncu summary (profiles/*_traffic.json)."""
     name = {("spmv", False): "spmv_fp64", ("spmv", True): "spmv_fp32", ("spmv6", True): "spmv6_fp32"}.get((family, fp32))
-    if name and fp32 and sym:
-        name += "_sym"
     p = os.path.join(ROOT, "profiles", f"{name}_traffic.json") if name else ""
     if name and os.path.exists(p):
         d = json.load(open(p))
@@ -307,7 +305,6 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     for h in handles:
         h.update_vars()
     nonlinear = sum(h.is_non_linear(gp) for h, gp in points)
-    sym32 = handles[0].ell32_symmetric()
     strain_bufs = [np.ascontiguousarray(t, dtype=np.float64) for t in tg]
     out_s = np.zeros((R, 6))
     out_c = np.zeros((R, 36))
@@ -364,7 +361,7 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     dev_s = max_over_ranks(pg, dev_ms / 1e3, world)
     wall_s = max_over_ranks(pg, wall, world)
     homs = R * args.steps * world
-    return {"form": form, "batched": batched, "sym32": sym32, "value": homs / dev_s, "e2e": homs / wall_s, "dev_s": dev_s,
+    return {"form": form, "batched": batched, "value": homs / dev_s, "e2e": homs / wall_s, "dev_s": dev_s,
             "wall_s": wall_s, "cg_its": cg_its, "launches": launches, "stats": stats, "clocks": clk.summary(),
             "nonlinear": nonlinear, "status": status, "newton": newton, "finite": finite, "stress": out_s.copy(),
             "ctan": out_c.copy()}
@@ -378,18 +375,15 @@ def roofline_of(res, n, peak, peak_kind):
     fam = max(cands, key=lambda k: cands[k][1])
     nk, ms, by = cands[fam]
     achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
-    # algorithmic bytes of one RVE's SpMV: the stored values once (81 per row, or 42 per row for the symmetric
-    # half), x read once, y written once (per right-hand side)
-    vpr = 42 if res.get("sym32") else 81
-    store = "symmetric half" if res.get("sym32") else "full stencil"
+    # algorithmic bytes of one RVE's SpMV: 81 values per row, x read once, y written once (per right-hand side)
     if fam == "spmv6":
-        name, per = f"k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides, {store})", nrow * (vpr * 4 + 12 * 4)
+        name, per = "k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides)", nrow * (81 * 4 + 12 * 4)
     elif fp32:
-        name, per = f"k_cg32_spmv (FP32 ELL SpMV + p.Ap, {store})", nrow * (vpr * 4 + 2 * 4)
+        name, per = "k_cg32_spmv (FP32 ELL SpMV + p.Ap)", nrow * (81 * 4 + 2 * 4)
     else:
         name, per = "k_cg_spmv (FP64 ELL SpMV + p.Ap)", nrow * (81 * 8 + 2 * 8)
     rves_per_launch = by / nk / per if nk else None
-    traffic = load_traffic(n, fam, fp32, bool(res.get("sym32")))  # DRAM bytes of one RVE's SpMV (ncu)
+    traffic = load_traffic(n, fam, fp32)  # DRAM bytes of one RVE's SpMV (ncu)
     if traffic is not None and rves_per_launch:
         traffic *= rves_per_launch
     return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -141,11 +141,6 @@ int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, cons
 long micropp3_total_cg_its(const struct micropp3 *self);
 long micropp3_kernel_launches(const struct micropp3 *self);
 
-/* 1 when the handle's FP32 Jacobian (mixed precision or implicit ctan) is stored as its symmetric half: every
- * phase has a symmetric consistent tangent (elastic, damage).  0 for the full stencil (a J2 phase, or no
- * FP32 Jacobian). */
-int micropp3_ell32_symmetric(const struct micropp3 *self);
-
 #ifdef __cplusplus
 }
 #endif

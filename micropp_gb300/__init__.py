@@ -109,7 +109,6 @@ def load():
         "micropp3_kernel_stats": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_long), dp, dp]),
         "micropp3_total_cg_its": (C.c_long, [H]),
         "micropp3_kernel_launches": (C.c_long, [H]),
-        "micropp3_ell32_symmetric": (C.c_int, [H]),
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
         "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                              C.c_int, ip, C.c_void_p]),
@@ -307,6 +306,3 @@ class Micropp:
 
     def kernel_launches(self):
         return self._call("micropp3_kernel_launches")
-
-    def ell32_symmetric(self):
-        return bool(self._call("micropp3_ell32_symmetric"))

@@ -12,11 +12,9 @@
 //                                            implicit; boundary rows are identity rows and are not stored.
 //   element residual blocks be               24 * nelem doubles, [(a*3+d) * nelem + e]
 //   internal variables                       7 doubles per Gauss point, [(e*8 + g)*7 + v] (params.hpp:41)
-// Mixed form: the same ELL layout in FP32 (vals32) with FP32 CG vectors.  When every phase has a symmetric
-// tangent (elastic, damage), vals32 holds only the 14 "upper" stencil slots s = 13..26 (self and the
-// neighbours after it in (dz,dy,dx) order) at [((s-13)*9 + fi*3 + fj) * np + n], for every node including
-// boundary nodes; the block of a lower slot s of node n is the transpose of slot 26-s of its neighbour.
-// The rest of the mixed form: the six tangent right-hand sides
+// Mixed form: the same ELL layout in FP32 (vals32) with FP32 CG vectors.  When every phase is elastic or
+// damage, vals32 is assembled by node gather and also holds the real rows of the boundary nodes (the CG still
+// treats them as identity rows); they give the ctan from the boundary reactions.  The rest of the mixed form: the six tangent right-hand sides
 // of the implicit ctan are stored component-major, [(i*3 + d) * np + n] (18 * np values), so that a warp
 // reading one component of 32 consecutive nodes touches 128 contiguous bytes.
 #pragma once
@@ -40,7 +38,6 @@ constexpr int kEllPerNode = 243;  // 27 stencil nodes x 3 x 3
 struct MeshDev {
   int nx, ny, nz, nxny, nn, np;  // np: padded node stride of the ELL arrays
   int nex, ney, nez, nelem;
-  int sym32, pad_;               // 1: the FP32 ELL holds the symmetric half (see kSymSlots)
   double lx, ly, lz, dx, dy, dz, wg, vol_tot;
 };
 
@@ -114,8 +111,6 @@ struct Inst {
 constexpr int kRedStride = 40;
 constexpr int kNodeBlock = 256;
 constexpr int kElemBlock = 128;
-
-constexpr int kSymSlots = 14;
 
 // Offset of component (i, d) of a 6-RHS vector.
 MGB_HD size_t c6(int i, int d, size_t np) { return (size_t)(i * 3 + d) * np; }

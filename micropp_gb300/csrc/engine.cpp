@@ -92,11 +92,11 @@ Engine::Engine(const micropp3_config &cfg) {
   build_elem_types(cfg);
   build_materials(cfg);
   build_phase_stiffness();
-  // The FP32 Jacobian (mixed precision or implicit ctan) is stored as its symmetric half when every phase
-  // in use has a symmetric consistent tangent (elastic, damage); a J2 phase keeps the full stencil.
-  sym32_ = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
-  for (int e = 0; e < mesh_.nelem && sym32_; ++e) sym32_ = mats_.m[etype_[e]].type != 1;
-  mesh_.sym32 = sym32_ ? 1 : 0;
+  // The FP32 Jacobian (mixed precision or implicit ctan) is assembled by node gather from the residual's
+  // Gauss-point tangent terms when every phase in use is elastic or damage; a J2 phase keeps the element
+  // colouring assembly.
+  gather32_ = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
+  for (int e = 0; e < mesh_.nelem && gather32_; ++e) gather32_ = mats_.m[etype_[e]].type != 1;
 
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   check(cudaEventCreate(&ev0_), "event");
@@ -118,6 +118,16 @@ Engine::Engine(const micropp3_config &cfg) {
     for (int i = 0; i < 192; ++i) dsh32[i] = (float)dsh_[i];
     d_dsh32_ = dalloc<float>(192, "dsh32");
     check(cudaMemcpy(d_dsh32_, dsh32, sizeof(dsh32), cudaMemcpyHostToDevice), "dsh32 upload");
+  }
+  if (gather32_) {
+    std::vector<int> bn;
+    for (int n = 0; n < mesh_.nn; ++n) {
+      const int i = n % mesh_.nx, j = (n / mesh_.nx) % mesh_.ny, k = n / mesh_.nxny;
+      if (i == 0 || j == 0 || k == 0 || i == mesh_.nx - 1 || j == mesh_.ny - 1 || k == mesh_.nz - 1) bn.push_back(n);
+    }
+    nbnodes_ = (int)bn.size();
+    d_bnodes_ = dalloc<int>(bn.size(), "boundary nodes");
+    check(cudaMemcpy(d_bnodes_, bn.data(), bn.size() * sizeof(int), cudaMemcpyHostToDevice), "boundary nodes upload");
   }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
@@ -181,6 +191,7 @@ Engine::~Engine() {
   dfree(d_ke32_);
   dfree(d_k0g32_);
   dfree(d_dsh32_);
+  dfree(d_bnodes_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -364,7 +375,7 @@ double Engine::slot_bytes() const {
   double b = 8.0 * (3.0 * nd + 24.0 * mesh_.nelem + nvars());  // u, du, b, be, vars_aux
   if (precision_ == MICROPP3_FP64) b += 8.0 * (kEllPerNode * np + 5.0 * nd);
   if (precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT)
-    b += 4.0 * ((sym32_ ? kSymSlots * 9 : kEllPerNode) * np + nd + (sym32_ ? 64.0 * mesh_.nelem : 0.0));
+    b += 4.0 * (kEllPerNode * np + nd + (gather32_ ? 64.0 * mesh_.nelem : 0.0));
   if (precision_ == MICROPP3_MIXED) b += 4.0 * 5.0 * nd;
   if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += (8.0 * 2.0 + 4.0 * 5.0) * 18.0 * np;
   return b;
@@ -400,9 +411,9 @@ void Engine::ensure_slots(int n) {
       w.vals = dalloc<double>((size_t)kEllPerNode * mesh_.np, "ELL values");
     }
     if (mixed || implicit) {
-      w.vals32 = dalloc<float>((size_t)(sym32_ ? kSymSlots * 9 : kEllPerNode) * mesh_.np, "ELL values (FP32)");
+      w.vals32 = dalloc<float>((size_t)kEllPerNode * mesh_.np, "ELL values (FP32)");
       w.kinv32 = dalloc<float>(nd, "kinv32");
-      if (sym32_) w.gpd = dalloc<float>((size_t)64 * mesh_.nelem, "Gauss-point tangent terms");
+      if (gather32_) w.gpd = dalloc<float>((size_t)64 * mesh_.nelem, "Gauss-point tangent terms");
     }
     if (mixed) {
       w.r32 = dalloc<float>(nd, "r32");
@@ -635,8 +646,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   launches_ += 1;
   check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
   const double nrow = (double)nndim();
-  // per iteration and instance, as in cg_solve; the symmetric half stores 42 values per row
-  const double spmv_bytes = nrow * ((sym32_ ? 42.0 : 81.0) * 4 + 2.0 * 4);
+  const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 4);  // per iteration and instance, as in cg_solve
   const double upd_bytes = nrow * 11.0 * 4;
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
@@ -664,15 +674,15 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   }
 }
 
-// Algorithmic bytes: the values written once; full stencil: u and the history read once per element;
-// symmetric half: the Gauss-point tangent terms (8 floats per Gauss point of a damage element) read once.
+// Algorithmic bytes: the values written once, plus u and the history read once per element (colouring) or
+// the Gauss-point tangent terms (8 floats per Gauss point) read once (gather).
 void Engine::assemble32(int nlist) {
-  if (sym32_) {
-    timer_begin(t_asm_, (double)nlist * (4.0 * kSymSlots * 9 * mesh_.np + 4.0 * 64.0 * mesh_.nelem));
+  if (gather32_) {
+    timer_begin(t_asm_, (double)nlist * (4.0 * kEllPerNode * mesh_.np + 4.0 * 64.0 * mesh_.nelem));
     launches_ += 1;
-    check_launch(mgb_launch_assembly_sym32(&mesh_, &mats_, d_etype_, d_k0g32_, d_ke32_, d_dsh32_, d_insts_, d_list_,
-                                           nlist, stream_),
-                 "assembly (symmetric FP32)");
+    check_launch(mgb_launch_assembly_gather32(&mesh_, &mats_, d_etype_, d_k0g32_, d_ke32_, d_dsh32_, d_insts_,
+                                              d_list_, nlist, stream_),
+                 "assembly (FP32 gather)");
   } else {
     timer_begin(t_asm_, (double)nlist * (4.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
     launches_ += 9;
@@ -696,7 +706,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   const double nrow = (double)nndim();
   // Per iteration and instance: SpMV 81 values per row, 6 x read and 6 y written; update: read P, AP, R, D,
   // write D, R, Z; p-update: read Z, P, write P (per right-hand side).  Credited per instance iteration.
-  const double spmv_bytes = nrow * ((sym32_ ? 42.0 : 81.0) * 4 + 2.0 * 6 * 4);
+  const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 6 * 4);
   const double upd6_bytes = nrow * 6.0 * 10.0 * 4;
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   std::vector<int> live = slots;
@@ -712,7 +722,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
     }
     if (sweep > 0) upload_list(live);
     launches_ += 1;
-    check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), stream_), "tangent residual");
+    check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0, stream_),
+                 "tangent residual");
     download_out();
     std::vector<int> next, next_idx;
     for (size_t a = 0; a < live.size(); ++a) {
@@ -738,7 +749,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
         check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
       }
       launches_ += 1;
-      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), stream_), "tangent residual");
+      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0, stream_),
+                   "tangent residual");
     }
     const int nl = (int)live.size();
     int done_its = 0;
@@ -771,7 +783,10 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   }
   upload_list(slots);
   launches_ += 1;
-  check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
+  if (gather32_)
+    check_launch(mgb_launch_ctan_react(&mesh_, d_bnodes_, nbnodes_, d_insts_, d_list_, n, stream_), "ctan reactions");
+  else
+    check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
   download_out();
   return its;
 }

@@ -105,7 +105,6 @@ class Engine {
   bool kernel_stats(const std::string &family, long *launches, double *ms, double *bytes);
   long total_cg_its() const { return total_cg_its_; }
   long kernel_launches() const { return launches_; }
-  bool ell32_symmetric() const { return sym32_; }
   int mpi_rank() const { return mpi_rank_; }
 
  private:
@@ -160,7 +159,7 @@ class Engine {
   double dsh_[8 * 24];
   double ke_phase_[3][576];
   std::vector<float> k0g32_;  // wg B_g^T C_phase B_g in FP32, [3][8][576]
-  bool sym32_ = false;        // the FP32 Jacobian is symmetric and stored as its upper half
+  bool gather32_ = false;     // the FP32 Jacobian is assembled by node gather (every phase elastic or damage)
   std::vector<int8_t> etype_;
   double Vm_ = 0, Vf_ = 0;
   double ctan_lin_[36] = {0};
@@ -171,6 +170,8 @@ class Engine {
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
   float *d_ke32_ = nullptr, *d_k0g32_ = nullptr, *d_dsh32_ = nullptr;
+  int *d_bnodes_ = nullptr;  // boundary nodes (gathered FP32 Jacobian: ctan from the boundary reactions)
+  int nbnodes_ = 0;
   std::vector<Slot> slots_;
   std::vector<Inst> h_insts_;
   Inst *d_insts_ = nullptr;

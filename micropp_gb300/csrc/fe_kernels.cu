@@ -354,61 +354,50 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Symmetric FP32 Jacobian by node gather (mixed form, every phase elastic or damage).
+// FP32 Jacobian by node gather (mixed form, every phase elastic or damage).
 //
 // Thread (node n, element position ep): of the 8 elements around n it takes the one at ep = dxq + 2 dyq +
 // 4 dzq, element (i-1+dxq, j-1+dyq, k-1+dzq), in which n is the local corner a = (1-dxq, 1-dyq, 1-dzq).  It
-// forms the 3x3 blocks of that element's matrix coupling a with every corner b at an upper slot of n:
+// forms the 3x3 blocks of that element's matrix coupling a with every corner b of the element:
 //   damage  (C_g = a_g C + c_g s_g s_g^T):  Ke_ab = sum_g a_g K0_g,ab + c_g wg (B_a,g^T s_g)(B_b,g^T s_g)^T
 //   elastic:                               Ke_ab = sum_g K0_g,ab
 // with K0_g = wg B_g^T C_phase B_g precomputed per phase and Gauss point, and (a_g, c_g, s_g) written by the
 // FP64 residual at the same displacement.  The 8 warps of a block (one element position each) add their
-// blocks into the block's 32 node rows in shared memory in a fixed order; the rows are then written once,
-// coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their full rows (the lower-slot
-// blocks of their interior neighbours are read from them).
+// blocks into the block's 32 node rows (27 slots x 9) in shared memory in a fixed order; the rows are then
+// written once, coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their real rows.
 constexpr int kAsmNodes = 32;
-constexpr int kAsmRow = kSymSlots * 9 + 1;  // 127 floats: odd stride, conflict-free
+constexpr int kAsmRow = kEllPerNode + 2;  // 245 floats: odd stride, conflict-free
 
 __host__ __device__ constexpr int corner_x(int b) { return ((b & 3) == 1 || (b & 3) == 2) ? 1 : 0; }
 __host__ __device__ constexpr int corner_y(int b) { return (b & 3) >= 2 ? 1 : 0; }
 __host__ __device__ constexpr int corner_z(int b) { return b >> 2; }
 __host__ __device__ constexpr int local_c(int ox, int oy, int oz) { return oz * 4 + (oy ? 3 - ox : ox); }
-// Upper-slot index (0..13) of the neighbour at offset (dx,dy,dz), or -1 for a lower slot.
-__host__ __device__ constexpr int sym_slot(int dx, int dy, int dz) {
-  return ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1) >= 13) ? (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1) - 13 : -1;
-}
-template <int A, int B>
-struct SymPair {
-  static constexpr int slot = sym_slot(corner_x(B) - corner_x(A), corner_y(B) - corner_y(A), corner_z(B) - corner_z(A));
-};
+// Stencil slot (0..26) of the neighbour at offset (dx,dy,dz).
+__host__ __device__ constexpr int slot_of(int dx, int dy, int dz) { return (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1); }
 
 template <int EP, int B>
 __device__ __forceinline__ void asm_add_b(float (&acc)[8][9], float A, float cw, const float (&va)[3],
                                           const float *dg, const float (&s)[6], const float *__restrict__ K) {
   constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
-  if constexpr (SymPair<a, B>::slot >= 0) {
-    const float gx = dg[B * 3], gy = dg[B * 3 + 1], gz = dg[B * 3 + 2];
-    const float vb[3] = {gx * s[0] + gy * s[3] + gz * s[4], gy * s[1] + gx * s[3] + gz * s[5],
-                         gz * s[2] + gx * s[4] + gy * s[5]};
+  const float gx = dg[B * 3], gy = dg[B * 3 + 1], gz = dg[B * 3 + 2];
+  const float vb[3] = {gx * s[0] + gy * s[3] + gz * s[4], gy * s[1] + gx * s[3] + gz * s[5],
+                       gz * s[2] + gx * s[4] + gy * s[5]};
 #pragma unroll
-    for (int fi = 0; fi < 3; ++fi)
+  for (int fi = 0; fi < 3; ++fi)
 #pragma unroll
-      for (int fj = 0; fj < 3; ++fj)
-        acc[B][fi * 3 + fj] += A * __ldg(&K[(a * 3 + fi) * 24 + B * 3 + fj]) + cw * va[fi] * vb[fj];
-  }
+    for (int fj = 0; fj < 3; ++fj)
+      acc[B][fi * 3 + fj] += A * __ldg(&K[(a * 3 + fi) * 24 + B * 3 + fj]) + cw * va[fi] * vb[fj];
 }
 
 template <int EP, int B>
 __device__ __forceinline__ void asm_add_b_elastic(float (&acc)[8][9], const float *__restrict__ K) {
   constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
-  if constexpr (SymPair<a, B>::slot >= 0) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[B][q] += __ldg(&K[(a * 3 + q / 3) * 24 + B * 3 + q % 3]);
-  }
+  for (int q = 0; q < 9; ++q) acc[B][q] += __ldg(&K[(a * 3 + q / 3) * 24 + B * 3 + q % 3]);
 }
 
 template <int EP>
-__device__ __forceinline__ void asm_sym_ep(const MeshDev &m, const Mats &mats, const int8_t *__restrict__ etype,
+__device__ __forceinline__ void asm_ep(const MeshDev &m, const Mats &mats, const int8_t *__restrict__ etype,
                                            const float *__restrict__ k0g, const float *__restrict__ kesum,
                                            const float *dsh, const float *__restrict__ gpd, int i, int j, int k,
                                            float (&acc)[8][9]) {
@@ -447,14 +436,13 @@ __device__ __forceinline__ void asm_sym_ep(const MeshDev &m, const Mats &mats, c
 }
 
 template <int EP>
-__device__ __forceinline__ void asm_sym_store(const float (&acc)[8][9], float *row) {
+__device__ __forceinline__ void asm_store(const float (&acc)[8][9], float *row) {
   constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
 #pragma unroll
   for (int b = 0; b < 8; ++b) {
-    const int sl = sym_slot(corner_x(b) - corner_x(a), corner_y(b) - corner_y(a), corner_z(b) - corner_z(a));
-    if (sl >= 0)
+    const int sl = slot_of(corner_x(b) - corner_x(a), corner_y(b) - corner_y(a), corner_z(b) - corner_z(a));
 #pragma unroll
-      for (int q = 0; q < 9; ++q) row[sl * 9 + q] += acc[b][q];
+    for (int q = 0; q < 9; ++q) row[sl * 9 + q] += acc[b][q];
   }
 }
 
@@ -470,7 +458,7 @@ __device__ __forceinline__ void asm_sym_store(const float (&acc)[8][9], float *r
     default: CALL(7); break;   \
   }
 
-__global__ void __launch_bounds__(kAsmNodes * 8) k_asm_sym32(MeshDev m, Mats mats, const int8_t *etype,
+__global__ void __launch_bounds__(kAsmNodes * 8) k_asm_gather32(MeshDev m, Mats mats, const int8_t *etype,
                                                               const float *k0g, const float *kesum,
                                                               const float *dsh_g, const Inst *insts,
                                                               const int *list) {
@@ -490,7 +478,7 @@ __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_sym32(MeshDev m, Mats mat
 #pragma unroll
     for (int q = 0; q < 9; ++q) acc[b][q] = 0.f;
   if (valid) {
-#define MGB_ASM_CALL(E) asm_sym_ep<E>(m, mats, etype, k0g, kesum, dsh, I.gpd, i, j, k, acc)
+#define MGB_ASM_CALL(E) asm_ep<E>(m, mats, etype, k0g, kesum, dsh, I.gpd, i, j, k, acc)
     MGB_EP_SWITCH(w, MGB_ASM_CALL)
 #undef MGB_ASM_CALL
   }
@@ -498,7 +486,7 @@ __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_sym32(MeshDev m, Mats mat
   for (int p = 0; p < 8; ++p) {
     __syncthreads();
     if (w == p && valid) {
-#define MGB_STORE_CALL(E) asm_sym_store<E>(acc, &rows[lane * kAsmRow])
+#define MGB_STORE_CALL(E) asm_store<E>(acc, &rows[lane * kAsmRow])
       MGB_EP_SWITCH(w, MGB_STORE_CALL)
 #undef MGB_STORE_CALL
     }
@@ -506,7 +494,7 @@ __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_sym32(MeshDev m, Mats mat
   __syncthreads();
   float *__restrict__ vals = I.vals32;
   const size_t np = m.np;
-  for (int E = w; E < kSymSlots * 9; E += 8) vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = rows[lane * kAsmRow + E];
+  for (int E = w; E < kEllPerNode; E += 8) vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = rows[lane * kAsmRow + E];
 }
 
 // Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
@@ -654,11 +642,11 @@ int mgb_launch_assembly32(const MeshDev *m, const Mats *mats, const int8_t *etyp
   return launch_assembly<float>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
 }
 
-int mgb_launch_assembly_sym32(const MeshDev *m, const Mats *mats, const int8_t *etype, const float *k0g,
+int mgb_launch_assembly_gather32(const MeshDev *m, const Mats *mats, const int8_t *etype, const float *k0g,
                               const float *kesum, const float *dsh32, const Inst *insts, const int *list, int nlist,
                               cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_asm_sym32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, 0, s>>>(*m, *mats, etype, k0g, kesum, dsh32,
+  k_asm_gather32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, 0, s>>>(*m, *mats, etype, k0g, kesum, dsh32,
                                                                              insts, list);
   return (int)cudaGetLastError();
 }

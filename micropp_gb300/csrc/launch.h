@@ -34,9 +34,9 @@ int mgb_launch_cg_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const i
 
 int mgb_launch_assembly32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                           const float *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
-// Symmetric FP32 Jacobian (every phase elastic or damage): k0g = wg B_g^T C B_g per phase and Gauss point
-// [3][8][576], kesum = its sum over g per phase [3][576], dsh32 = the shape-function gradients [8][24].
-int mgb_launch_assembly_sym32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *k0g,
+// FP32 Jacobian by node gather (every phase elastic or damage): k0g = wg B_g^T C B_g per phase and Gauss
+// point [3][8][576], kesum = its sum over g per phase [3][576], dsh32 = the shape-function gradients [8][24].
+int mgb_launch_assembly_gather32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *k0g,
                               const float *kesum, const float *dsh32, const mgb::Inst *insts, const int *list,
                               int nlist, cudaStream_t s);
 int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
@@ -46,13 +46,18 @@ int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const
                             unsigned int *active_count, cudaStream_t s);
 int mgb_launch_add_du32(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
-int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
+                           cudaStream_t s);
 int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg6_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg6_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s);
 int mgb_launch_t6_accumulate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                              cudaStream_t s);
+// ctan from the boundary reactions of the tangent fields (gather-assembled FP32 Jacobian); bnodes lists the nbn
+// boundary nodes.
+int mgb_launch_ctan_react(const mgb::MeshDev *m, const int *bnodes, int nbn, const mgb::Inst *insts, const int *list,
+                          int nlist, cudaStream_t s);
 int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 

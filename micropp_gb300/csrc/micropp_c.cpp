@@ -260,11 +260,6 @@ long micropp3_kernel_launches(const struct micropp3 *self) {
   return e ? e->kernel_launches() : 0;
 }
 
-int micropp3_ell32_symmetric(const struct micropp3 *self) {
-  Engine *e = eng(self, "micropp3_ell32_symmetric");
-  return e && e->ell32_symmetric() ? 1 : 0;
-}
-
 long micropp3_total_cg_its(const struct micropp3 *self) {
   Engine *e = eng(self, "micropp3_total_cg_its");
   return e ? e->total_cg_its() : 0;

@@ -68,57 +68,16 @@ __device__ __forceinline__ int nb_of(const MeshDev &m, int n, int s) {
   return n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
 }
 
-// The 3x3 block (row-major fi, fj) of FP32 ELL row n at stencil slot s, whose neighbour is nb, from either
-// storage: the full stencil, or the symmetric half, where a lower slot s is the transpose of slot 26 - s of
-// the neighbour's row.
+// The 3x3 block (row-major fi, fj) of FP32 ELL row n at stencil slot s.
 template <typename T>
-__device__ __forceinline__ void ell32_block(const MeshDev &m, const float *__restrict__ vals, int n, int nb, int s,
-                                            T (&K)[9]) {
-  const size_t np = m.np;
-  if (!m.sym32) {
+__device__ __forceinline__ void ell32_block(const MeshDev &m, const float *__restrict__ vals, int n, int s, T (&K)[9]) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) K[q] = (T)vals[(size_t)(s * 9 + q) * np + n];
-  } else if (s >= 13) {
-#pragma unroll
-    for (int q = 0; q < 9; ++q) K[q] = (T)vals[(size_t)((s - 13) * 9 + q) * np + n];
-  } else {
-#pragma unroll
-    for (int fi = 0; fi < 3; ++fi)
-#pragma unroll
-      for (int fj = 0; fj < 3; ++fj) K[fi * 3 + fj] = (T)vals[(size_t)((13 - s) * 9 + fj * 3 + fi) * np + nb];
-  }
-}
-
-// Four consecutive floats starting R floats into the 8 loaded as lo, hi (R uniform over the grid).
-template <int R>
-__device__ __forceinline__ float4 shift4(const float4 lo, const float4 hi) {
-  if constexpr (R == 0) return lo;
-  else if constexpr (R == 1) return make_float4(lo.y, lo.z, lo.w, hi.x);
-  else if constexpr (R == 2) return make_float4(lo.z, lo.w, hi.x, hi.y);
-  else return make_float4(lo.w, hi.x, hi.y, hi.z);
-}
-
-// Lower-slot contribution of the symmetric FP32 ELL to 4 consecutive rows n0..n0+3: the rows' block at slot
-// sl is the transpose of block 13 - sl of rows a0 + R .. a0 + R + 3 (a0 = n0 + doff - R, 16-byte aligned),
-// read as two aligned 16-byte loads per entry.
-template <int R>
-__device__ __forceinline__ void lower4(const float *__restrict__ vt, size_t np, int a0, const float (&x)[6][3],
-                                       int dx, float (&y)[4][3]) {
-#pragma unroll
-  for (int e = 0; e < 9; ++e) {
-    const int fi = e / 3, fj = e % 3;
-    const float4 *row = reinterpret_cast<const float4 *>(vt + (size_t)(fj * 3 + fi) * np + a0);
-    const float4 t = shift4<R>(__ldg(row), __ldg(row + 1));
-    y[0][fi] = fmaf(t.x, x[0 + dx][fj], y[0][fi]);
-    y[1][fi] = fmaf(t.y, x[1 + dx][fj], y[1][fi]);
-    y[2][fi] = fmaf(t.z, x[2 + dx][fj], y[2][fi]);
-    y[3][fi] = fmaf(t.w, x[3 + dx][fj], y[3][fi]);
-  }
+  for (int q = 0; q < 9; ++q) K[q] = (T)vals[(size_t)(s * 9 + q) * m.np + n];
 }
 
 // Entry index of diagonal entry (d, d) of row n's own block in the FP32 ELL.
 __device__ __forceinline__ size_t ell32_diag(const MeshDev &m, int n, int d) {
-  return (size_t)((m.sym32 ? 0 : 13 * 9) + d * 3 + d) * m.np + n;
+  return (size_t)(13 * 9 + d * 3 + d) * m.np + n;
 }
 
 }  // namespace
@@ -180,12 +139,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
   }
 }
 
-// Ap = K p for kSpmvNodes consecutive nodes per thread.  Each stored ELL entry of the group is one 16-byte
-// load (np is a multiple of 32 and the group starts at a multiple of 4), and the 6 neighbours a group row
-// needs along x are loaded once for the 3 x-slots.  Sym: the 13 lower slots are read transposed from the
-// neighbours' rows (scalar loads, mostly L2 hits: those rows are streamed by nearby blocks).  A boundary node
-// of the group is an identity row: its stencil sum (over clamped neighbour indices) is discarded.
-template <bool Sym>
+// Ap = K p for kSpmvNodes consecutive nodes per thread.  Each ELL entry of the group is one 16-byte load
+// (np is a multiple of 32 and the group starts at a multiple of 4), and the 6 neighbours a group row needs
+// along x are loaded once for the 3 x-slots.  A boundary node of the group is an identity row: its stencil
+// sum (taken over clamped neighbour indices) is discarded.
 __global__ void __launch_bounds__(kSpmvBlock) k_cg32_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg->done) return;
@@ -206,58 +163,31 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg32_spmv(MeshDev m, const Inst 
 #pragma unroll
     for (int q = 0; q < kSpmvNodes; ++q) y[q][0] = y[q][1] = y[q][2] = 0.f;
     if (any_interior) {
-      const size_t np = m.np, np4 = np / 4;
-      const float *__restrict__ vals = I.vals32;
-      const float4 *__restrict__ v4 = reinterpret_cast<const float4 *>(vals + n0);
+      const size_t np4 = (size_t)m.np / 4;
+      const float4 *__restrict__ v4 = reinterpret_cast<const float4 *>(I.vals32 + n0);
       const int last = m.nn - 1;
 #pragma unroll 1
       for (int zy = 0; zy < 9; ++zy) {
         const int base = n0 + (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx - 1;
         float x[kSpmvNodes + 2][3];
-        int nbw[kSpmvNodes + 2];
 #pragma unroll
         for (int w = 0; w < kSpmvNodes + 2; ++w) {
           const int nb = min(max(base + w, 0), last);
-          nbw[w] = nb;
           x[w][0] = p[nb * 3 + 0];
           x[w][1] = p[nb * 3 + 1];
           x[w][2] = p[nb * 3 + 2];
         }
 #pragma unroll
         for (int dx = 0; dx < 3; ++dx) {
-          const int sl = zy * 3 + dx;
-          if (!Sym || sl >= 13) {
-            const float4 *vs = v4 + (size_t)((Sym ? sl - 13 : sl) * 9) * np4;
+          const float4 *vs = v4 + (size_t)((zy * 3 + dx) * 9) * np4;
 #pragma unroll
-            for (int e = 0; e < 9; ++e) {
-              const float4 a = Sym ? __ldg(vs + e * np4) : __ldcs(vs + e * np4);
-              const int fi = e / 3, fj = e % 3;
-              y[0][fi] = fmaf(a.x, x[0 + dx][fj], y[0][fi]);
-              y[1][fi] = fmaf(a.y, x[1 + dx][fj], y[1][fi]);
-              y[2][fi] = fmaf(a.z, x[2 + dx][fj], y[2][fi]);
-              y[3][fi] = fmaf(a.w, x[3 + dx][fj], y[3][fi]);
-            }
-          } else {
-            // lower slot: rows n0 + doff + q hold the transposed blocks; doff & 3 is the same for every group
-            const float *vt = vals + (size_t)((13 - sl) * 9) * np;
-            const int doff = (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx + (dx - 1);
-            const int r = doff & 3, a0 = n0 + doff - r;
-            if (a0 >= 0 && a0 + 8 <= m.np) {
-              if (r == 0) lower4<0>(vt, np, a0, x, dx, y);
-              else if (r == 1) lower4<1>(vt, np, a0, x, dx, y);
-              else if (r == 2) lower4<2>(vt, np, a0, x, dx, y);
-              else lower4<3>(vt, np, a0, x, dx, y);
-            } else {  // first or last groups of the array: clamped scalar loads
-#pragma unroll
-              for (int q = 0; q < kSpmvNodes; ++q) {
-                const float *vq = vt + nbw[q + dx];
-#pragma unroll
-                for (int e = 0; e < 9; ++e) {
-                  const int fi = e / 3, fj = e % 3;  // block (fi, fj) of row n0+q = entry (fj, fi) of the neighbour
-                  y[q][fi] = fmaf(__ldg(vq + (size_t)(fj * 3 + fi) * np), x[q + dx][fj], y[q][fi]);
-                }
-              }
-            }
+          for (int e = 0; e < 9; ++e) {
+            const float4 a = __ldcs(vs + e * np4);
+            const int fi = e / 3, fj = e % 3;
+            y[0][fi] = fmaf(a.x, x[0 + dx][fj], y[0][fi]);
+            y[1][fi] = fmaf(a.y, x[1 + dx][fj], y[1][fi]);
+            y[2][fi] = fmaf(a.z, x[2 + dx][fj], y[2][fi]);
+            y[3][fi] = fmaf(a.w, x[3 + dx][fj], y[3][fi]);
           }
         }
       }
@@ -401,7 +331,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
         double c[3];
         bc_coords(m, bi, bj, bk, c);
         double Kb[9];
-        ell32_block(m, I.vals32, n, nb, s, Kb);
+        ell32_block(m, I.vals32, n, s, Kb);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           double w[3];
@@ -434,8 +364,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
 }
 
 // Refinement residual RF = F - K X (FP64 accumulation), start of a 6-RHS CG on it:
-// R = RF (FP32), D = 0, Z = kinv R, P = Z; the last block initialises the six CG states.
-__global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Inst *insts, const int *list) {
+// R = RF (FP32), D = 0, Z = kinv R, P = Z; the last block initialises the six CG states.  x_zero: X is
+// still 0 (the first sweep), RF = F without the product.
+__global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Inst *insts, const int *list,
+                                                            int x_zero) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[18];
@@ -454,12 +386,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
     float kd[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) kd[d] = I.kinv32[n * 3 + d];
-    if (!b) {
+    if (!b && !x_zero) {
 #pragma unroll 1
       for (int s = 0; s < 27; ++s) {
         const int nb = nb_of(m, n, s);
         double Kb[9];
-        ell32_block(m, I.vals32, n, nb, s, Kb);
+        ell32_block(m, I.vals32, n, s, Kb);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           const double x0 = X6[c6(r, 0, np) + nb], x1 = X6[c6(r, 1, np) + nb], x2 = X6[c6(r, 2, np) + nb];
@@ -509,11 +441,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
   }
 }
 
-// AP = K P for the six right-hand sides, one pass over K for all six; kSpmv6Nodes consecutive nodes per
-// thread, so each stored ELL entry of the pair is one 8-byte load and the 4 neighbours a pair row needs
-// along x are loaded once for the 3 x-slots (Sym: lower slots transposed from the neighbours' rows, as in
-// k_cg32_spmv).  The last block sets alpha_i.
-template <bool Sym>
+// AP = K P for the six right-hand sides on the full stencil, one pass over K for all six; kSpmv6Nodes
+// consecutive nodes per thread, so each ELL entry of the pair is one 8-byte load and the 4 neighbours a pair
+// row needs along x are loaded once for the 3 x-slots.  The last block sets alpha_i.
 __global__ void __launch_bounds__(kSpmv6Block) k_cg6_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg6->all_done) return;
@@ -548,37 +478,9 @@ __global__ void __launch_bounds__(kSpmv6Block) k_cg6_spmv(MeshDev m, const Inst 
         for (int w = 0; w < kSpmv6Nodes + 2; ++w) nb[w] = min(max(base + w, 0), last);
         float2 a[3][9];
 #pragma unroll
-        for (int dx = 0; dx < 3; ++dx) {
-          const int sl = zy * 3 + dx;
-          if (!Sym) {
+        for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-            for (int e = 0; e < 9; ++e) a[dx][e] = __ldcs(v2 + (size_t)(sl * 9 + e) * np2);
-          } else if (sl >= 13) {
-#pragma unroll
-            for (int e = 0; e < 9; ++e) a[dx][e] = __ldg(v2 + (size_t)((sl - 13) * 9 + e) * np2);
-          } else {
-            // lower slot: rows n0 + doff + q (q = 0, 1) hold the transposed blocks; doff & 1 is uniform
-            const float *vt = I.vals32 + (size_t)((13 - sl) * 9) * np;
-            const int doff = (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx + (dx - 1);
-            const int r = doff & 1, a0 = n0 + doff - r;
-            if (a0 >= 0 && a0 + 4 <= m.np) {
-#pragma unroll
-              for (int e = 0; e < 9; ++e) {
-                const int fi = e / 3, fj = e % 3;
-                const float2 *row = reinterpret_cast<const float2 *>(vt + (size_t)(fj * 3 + fi) * np + a0);
-                const float2 lo = __ldg(row), hi = __ldg(row + 1);
-                a[dx][e] = r ? make_float2(lo.y, hi.x) : lo;
-              }
-            } else {
-#pragma unroll
-              for (int e = 0; e < 9; ++e) {
-                const int fi = e / 3, fj = e % 3;
-                a[dx][e].x = __ldg(vt + (size_t)(fj * 3 + fi) * np + nb[0 + dx]);
-                a[dx][e].y = __ldg(vt + (size_t)(fj * 3 + fi) * np + nb[1 + dx]);
-              }
-            }
-          }
-        }
+          for (int e = 0; e < 9; ++e) a[dx][e] = __ldcs(v2 + (size_t)((zy * 3 + dx) * 9 + e) * np2);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           float x[kSpmv6Nodes + 2][3];
@@ -620,8 +522,14 @@ __global__ void __launch_bounds__(kSpmv6Block) k_cg6_spmv(MeshDev m, const Inst 
   }
 }
 
-// D += alpha P; R -= alpha AP; Z = kinv R for the right-hand sides still iterating, one thread per node
-// (grid-stride); the last block sets beta_i and the stop flags.
+// The 6-RHS vector updates work on chunks of kVec6Chunk nodes, kVec6PerThread per thread (nodes strided by
+// the block size, so every access is coalesced).
+constexpr int kVec6PerThread = 4;
+constexpr int kVec6Chunk = kVec6PerThread * kNodeBlock;
+
+// D += alpha P; R -= alpha AP; Z = kinv R for the right-hand sides still iterating.  A block takes one node
+// chunk through the 18 components in turn (the 16 loads of a component in flight together); an instance has
+// nn / kVec6Chunk blocks to reduce, and the last one sets beta_i and the stop flags.
 __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const Cg6State *cs = I.cg6;
@@ -637,35 +545,45 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
 #pragma unroll
   for (int q = 0; q < 12; ++q) acc[q] = 0.f;  // [0,6): z.z  [6,12): r.z
   const size_t np = m.np;
-  float *__restrict__ D6 = I.D6;
-  float *__restrict__ R6 = I.R6;
-  float *__restrict__ Z6 = I.Z6;
-  const float *__restrict__ P6 = I.P6;
-  const float *__restrict__ AP6 = I.AP6;
-  const float *__restrict__ kinv = I.kinv32;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x) {
-    float kd[3];
+  const int n0 = blockIdx.x * kVec6Chunk + threadIdx.x;
+  float kd[kVec6PerThread][3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) kd[d] = kinv[n * 3 + d];
+  for (int q = 0; q < kVec6PerThread; ++q) {
+    const int n = n0 + q * kNodeBlock;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      if (!live[r]) continue;
-      float pv[3], av[3], rv[3], dv[3];
+    for (int d = 0; d < 3; ++d) kd[q][d] = (n < m.nn) ? I.kinv32[n * 3 + d] : 0.f;
+  }
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const size_t idx = c6(r, d, np) + n;
-        pv[d] = P6[idx]; av[d] = AP6[idx]; rv[d] = R6[idx]; dv[d] = D6[idx];
+  for (int r = 0; r < 6; ++r) {
+    if (!live[r]) continue;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const size_t off = c6(r, d, np);
+      float *__restrict__ D6 = I.D6 + off;
+      float *__restrict__ R6 = I.R6 + off;
+      float *__restrict__ Z6 = I.Z6 + off;
+      const float *__restrict__ P6 = I.P6 + off;
+      const float *__restrict__ AP6 = I.AP6 + off;
+      float pv[kVec6PerThread], av[kVec6PerThread], rv[kVec6PerThread], dv[kVec6PerThread];
+#pragma unroll
+      for (int q = 0; q < kVec6PerThread; ++q) {
+        const int n = n0 + q * kNodeBlock;
+        if (n < m.nn) {
+          pv[q] = P6[n]; av[q] = AP6[n]; rv[q] = R6[n]; dv[q] = D6[n];
+        }
       }
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const size_t idx = c6(r, d, np) + n;
-        D6[idx] = fmaf(alpha[r], pv[d], dv[d]);
-        const float rr = fmaf(-alpha[r], av[d], rv[d]);
-        const float z = kd[d] * rr;
-        R6[idx] = rr;
-        Z6[idx] = z;
-        acc[r] = fmaf(z, z, acc[r]);
-        acc[6 + r] = fmaf(rr, z, acc[6 + r]);
+      for (int q = 0; q < kVec6PerThread; ++q) {
+        const int n = n0 + q * kNodeBlock;
+        if (n < m.nn) {
+          D6[n] = fmaf(alpha[r], pv[q], dv[q]);
+          const float rr = fmaf(-alpha[r], av[q], rv[q]);
+          const float z = kd[q][d] * rr;
+          R6[n] = rr;
+          Z6[n] = z;
+          acc[r] = fmaf(z, z, acc[r]);
+          acc[6 + r] = fmaf(rr, z, acc[6 + r]);
+        }
       }
     }
   }
@@ -689,34 +607,36 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
   }
 }
 
+// P = Z + beta P for the right-hand sides still iterating, element-wise: block b of an instance handles
+// component c = b / nchunk of node chunk b % nchunk.
 __global__ void __launch_bounds__(kNodeBlock) k_cg6_pupdate(MeshDev m, const Inst *insts, const int *list,
                                                             unsigned int *active_count) {
   const Inst &I = insts[list[blockIdx.y]];
   const Cg6State *cs = I.cg6;
   if (cs->all_done) return;
-  float beta[6];
-  bool live[6];
-#pragma unroll
-  for (int r = 0; r < 6; ++r) {
-    beta[r] = (float)cs->beta[r];
-    live[r] = !cs->done[r];
-  }
-  const size_t np = m.np;
-  float *__restrict__ P6 = I.P6;
-  const float *__restrict__ Z6 = I.Z6;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x) {
-    float pv[18], zv[18];
-#pragma unroll
-    for (int c = 0; c < 18; ++c)
-      if (live[c / 3]) {
-        pv[c] = P6[(size_t)c * np + n];
-        zv[c] = Z6[(size_t)c * np + n];
-      }
-#pragma unroll
-    for (int c = 0; c < 18; ++c)
-      if (live[c / 3]) P6[(size_t)c * np + n] = fmaf(beta[c / 3], pv[c], zv[c]);
-  }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
+  const int nchunk = (m.nn + kVec6Chunk - 1) / kVec6Chunk;
+  const int c = blockIdx.x / nchunk, chunk = blockIdx.x - c * nchunk, r = c / 3;
+  if (cs->done[r]) return;
+  const float beta = (float)cs->beta[r];
+  const size_t off = (size_t)c * m.np;
+  float *__restrict__ P6 = I.P6 + off;
+  const float *__restrict__ Z6 = I.Z6 + off;
+  const int n0 = chunk * kVec6Chunk + threadIdx.x;
+  float pv[kVec6PerThread], zv[kVec6PerThread];
+#pragma unroll
+  for (int q = 0; q < kVec6PerThread; ++q) {
+    const int n = n0 + q * kNodeBlock;
+    if (n < m.nn) {
+      pv[q] = P6[n];
+      zv[q] = Z6[n];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kVec6PerThread; ++q) {
+    const int n = n0 + q * kNodeBlock;
+    if (n < m.nn) P6[n] = fmaf(beta, pv[q], zv[q]);
+  }
 }
 
 // X += D (FP64 accumulation of the FP32 correction), one thread per node.
@@ -728,6 +648,76 @@ __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x)
 #pragma unroll
     for (int c = 0; c < 18; ++c) X6[(size_t)c * np + n] += (double)D6[(size_t)c * np + n];
+}
+
+// ctan by boundary reactions (FP32 Jacobian assembled by node gather, which stores the boundary rows).  Column i of ctan
+// is the volume-average stress of the tangent field u_i = w_i + x_i, and for any displacement field
+//   integral of sigma = sum over all nodes n of f_n (x) X_n,   f_n = (K u)_n,
+// because the nodal gradients of the shape functions weighted by the nodal coordinates sum to the identity.
+// On interior rows f_n = -RF_n, the final refinement residual (below the tangent tolerance), so the sum runs
+// over the boundary nodes; the shear entries take the symmetric part.  One thread per boundary node, FP64
+// accumulation of the FP32 matrix values.
+__global__ void __launch_bounds__(kNodeBlock) k_ctan_react(MeshDev m, const int *bnodes, int nbn, const Inst *insts,
+                                                           const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[36];
+#pragma unroll
+  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
+  if (t < nbn) {
+    const int n = bnodes[t];
+    int i, j, k;
+    bnd(m, n, i, j, k);
+    double X[3];
+    bc_coords(m, i, j, k, X);
+    const size_t np = m.np;
+    double f[6][3];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) f[r][0] = f[r][1] = f[r][2] = 0.0;
+#pragma unroll 1
+    for (int s = 0; s < 27; ++s) {
+      const int di = s % 3 - 1, dj = (s / 3) % 3 - 1, dk = s / 9 - 1;
+      const int ii = i + di, jj = j + dj, kk = k + dk;
+      if (ii < 0 || jj < 0 || kk < 0 || ii >= m.nx || jj >= m.ny || kk >= m.nz) continue;
+      const int nb = n + dk * m.nxny + dj * m.nx + di;
+      double Kb[9];
+      ell32_block(m, I.vals32, n, s, Kb);
+      int bi, bj, bk;
+      const bool nbb = bnd(m, nb, bi, bj, bk);
+      double c[3];
+      if (nbb) bc_coords(m, bi, bj, bk, c);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        double u[3];
+        if (nbb) {
+          lift(c, r, u);
+        } else {
+#pragma unroll
+          for (int d = 0; d < 3; ++d) u[d] = I.X6[c6(r, d, np) + nb];
+        }
+#pragma unroll
+        for (int fi = 0; fi < 3; ++fi) f[r][fi] += Kb[fi * 3] * u[0] + Kb[fi * 3 + 1] * u[1] + Kb[fi * 3 + 2] * u[2];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      acc[0 * 6 + r] = f[r][0] * X[0];
+      acc[1 * 6 + r] = f[r][1] * X[1];
+      acc[2 * 6 + r] = f[r][2] * X[2];
+      acc[3 * 6 + r] = 0.5 * (f[r][0] * X[1] + f[r][1] * X[0]);
+      acc[4 * 6 + r] = 0.5 * (f[r][0] * X[2] + f[r][2] * X[0]);
+      acc[5 * 6 + r] = 0.5 * (f[r][1] * X[2] + f[r][2] * X[1]);
+    }
+  }
+  double tot[36];
+  if (grid_sum<36>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+    bool bad = false;
+    for (int q = 0; q < 36; ++q) {
+      I.out->ctan[q] = tot[q] / m.vol_tot;
+      bad |= !isfinite(tot[q]);
+    }
+    if (bad) I.out->nonfinite = 1;
+  }
 }
 
 // ctan[v][i] = (1/V) sum over Gauss points of wg (C_gp B (w_i + x_i))_v, one thread per Gauss point, FP64.
@@ -833,11 +823,7 @@ int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, 
 
 int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  const dim3 g(cdiv(cdiv(m->nn, kSpmvNodes), kSpmvBlock), nlist);
-  if (m->sym32)
-    k_cg32_spmv<true><<<g, kSpmvBlock, 0, s>>>(*m, insts, list);
-  else
-    k_cg32_spmv<false><<<g, kSpmvBlock, 0, s>>>(*m, insts, list);
+  k_cg32_spmv<<<dim3(cdiv(cdiv(m->nn, kSpmvNodes), kSpmvBlock), nlist), kSpmvBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
@@ -869,38 +855,42 @@ int mgb_launch_t6_rhs(const MeshDev *m, const Inst *insts, const int *list, int 
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, int x_zero,
+                           cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, x_zero);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  const dim3 g(cdiv(cdiv(m->nn, kSpmv6Nodes), kSpmv6Block), nlist);
-  if (m->sym32)
-    k_cg6_spmv<true><<<g, kSpmv6Block, 0, s>>>(*m, insts, list);
-  else
-    k_cg6_spmv<false><<<g, kSpmv6Block, 0, s>>>(*m, insts, list);
+  k_cg6_spmv<<<dim3(cdiv(cdiv(m->nn, kSpmv6Nodes), kSpmv6Block), nlist), kSpmv6Block, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_update<<<dim3(cdiv(m->nn, 2 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg6_update<<<dim3(cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_cg6_pupdate(const MeshDev *m, const Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_pupdate<<<dim3(cdiv(m->nn, 2 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
+  k_cg6_pupdate<<<dim3(18 * cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list, active_count);
   return (int)cudaGetLastError();
 }
 
 int mgb_launch_t6_accumulate(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
   k_t6_accumulate<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_ctan_react(const MeshDev *m, const int *bnodes, int nbn, const Inst *insts, const int *list, int nlist,
+                          cudaStream_t s) {
+  if (nlist <= 0 || nbn <= 0) return 0;
+  k_ctan_react<<<dim3(cdiv(nbn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, bnodes, nbn, insts, list);
   return (int)cudaGetLastError();
 }
 
