@@ -137,6 +137,22 @@ int micropp3_ell_solve_cgpd(const int nodes[3], const double *vals, const double
 int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, const double *b, double *x,
                                     double rel_tol, double abs_tol, int max_its, int *its, void *stream);
 
+/* Reverse-mode gradients of a load path (no counterpart in the reference, which has no derivatives other
+ * than ctan).  micropp3_path_forward runs the RVE of this handle from the undeformed state (zero history)
+ * through nsteps macro strains strains[nsteps][6], accepting every step, with the per-phase material
+ * parameters params[3][5] = (E, nu, Xt, Sy, Ka) in place of the handle's (phase types and all other settings
+ * are the handle's; Newton is the FP64 plain form at the handle's tolerances).  It writes the average stress
+ * of every step to sigma[nsteps][6] and keeps the state before every checkpoint_every-th step.
+ * micropp3_path_vjp then returns, for L = sum_n gsigma[n] . sigma[n], grad_params[3][5] = dL/dparams and, if
+ * grad_strains is not NULL, grad_strains[nsteps][6] = dL/dstrains[n]: an adjoint solve per step on the
+ * exact consistent tangent, the history sensitivities carried backwards, each segment recomputed from its
+ * checkpoint.  Entries of a parameter a phase's law does not use are 0.
+ * Both return 0, 1 when a Newton step (forward) or an adjoint solve (reverse) did not converge, -2 on an
+ * error (see micropp3_last_error). */
+int micropp3_path_forward(struct micropp3 *self, int nsteps, const double *strains, const double *params,
+                          int checkpoint_every, double *sigma);
+int micropp3_path_vjp(struct micropp3 *self, const double *gsigma, double *grad_params, double *grad_strains);
+
 /* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
 long micropp3_total_cg_its(const struct micropp3 *self);
 long micropp3_kernel_launches(const struct micropp3 *self);

@@ -109,6 +109,8 @@ def load():
         "micropp3_kernel_stats": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_long), dp, dp]),
         "micropp3_total_cg_its": (C.c_long, [H]),
         "micropp3_kernel_launches": (C.c_long, [H]),
+        "micropp3_path_forward": (C.c_int, [H, C.c_int, dp, dp, C.c_int, dp]),
+        "micropp3_path_vjp": (C.c_int, [H, dp, dp, dp]),
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
         "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                              C.c_int, ip, C.c_void_p]),
@@ -306,3 +308,20 @@ class Micropp:
 
     def kernel_launches(self):
         return self._call("micropp3_kernel_launches")
+
+    def path_forward(self, strains, params, checkpoint_every=5):
+        """Average stress of every step of a load path from the undeformed state (micropp3_path_forward).
+        strains: (nsteps, 6); params: (3, 5) = (E, nu, Xt, Sy, Ka) per phase.  Returns (sigma, status)."""
+        e = np.ascontiguousarray(strains, dtype=np.float64).reshape(-1, 6)
+        p = np.ascontiguousarray(params, dtype=np.float64).reshape(3, 5)
+        sig = np.zeros_like(e)
+        rc = self._call("micropp3_path_forward", e.shape[0], _dp(e), _dp(p), int(checkpoint_every), _dp(sig))
+        return sig, rc
+
+    def path_vjp(self, gsigma):
+        """dL/dparams (3, 5) and dL/dstrains (nsteps, 6) for L = sum gsigma . sigma of the last path."""
+        g = np.ascontiguousarray(gsigma, dtype=np.float64).reshape(-1, 6)
+        gp = np.zeros((3, 5))
+        gs = np.zeros_like(g)
+        rc = self._call("micropp3_path_vjp", _dp(g), _dp(gp), _dp(gs))
+        return gp, gs, rc

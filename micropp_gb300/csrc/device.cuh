@@ -108,6 +108,31 @@ struct Inst {
   int pad;
 };
 
+// Scalars of one BiCGSTAB solve (the adjoint system), resident on the device.
+struct BicgState {
+  double rho, rho_old, alpha, omega, beta, r0, rnorm, rel_tol;
+  int its, max_its, done, converged;
+};
+
+// Vectors and scratch of the adjoint solve of one RVE (node-interleaved FP64, like u).
+struct AdjDev {
+  double *x, *r, *rh, *p, *v, *s, *t, *y, *z, *kinv;
+  const double *b, *vals;
+  double *red;
+  unsigned int *ticket;
+  BicgState *st;
+};
+
+// One load step of the adjoint of a path (per-Gauss-point arrays in the history layout [(e*8+g)*7 + k]).
+struct AdjStep {
+  double g[6];          // dL / d(average stress) of the step
+  double wgv;           // Gauss weight / RVE volume
+  const double *mu_in;  // dL / d(history after the step), NULL for the last step
+  double *mu_out;       // dL / d(history before the step)
+  const double *lam;    // adjoint solution, node-interleaved
+  double *out;          // 21 sums: dL/dtheta of the 3 phases x 5, then dL/d(macro strain) (6)
+};
+
 constexpr int kRedStride = 40;
 constexpr int kNodeBlock = 256;
 constexpr int kElemBlock = 128;

@@ -15,6 +15,7 @@
 #include <sstream>
 #include <stdexcept>
 
+#include "cuda_util.hpp"
 #include "launch.h"
 #include "microstructure.hpp"
 
@@ -32,26 +33,6 @@ constexpr double kTangentTol = 1.0e-9;
 constexpr int kTangentSweeps = 4;
 
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-
-void check(cudaError_t e, const char *what) {
-  if (e != cudaSuccess) {
-    throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
-  }
-}
-
-void check_launch(int e, const char *what) { check((cudaError_t)e, what); }
-
-template <typename T>
-T *dalloc(size_t n, const char *what) {
-  void *p = nullptr;
-  if (n == 0) n = 1;
-  check(cudaMalloc(&p, n * sizeof(T)), what);
-  return (T *)p;
-}
-
-void dfree(void *p) {
-  if (p) cudaFree(p);
-}
 
 }  // namespace
 
@@ -179,6 +160,7 @@ Engine::~Engine() {
     dfree(g.vars_n);
     dfree(g.vars_k);
   }
+  path_free();
   free_slots();
   for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_})
     for (auto &e : t->pool) {
@@ -272,44 +254,53 @@ void Engine::build_elem_types(const micropp3_config &cfg) {
 }
 
 // Material constants with the expressions of material.hpp:73-135 and material.cpp:205-225.
+// Constants of one material for the device laws, by the reference's expressions (material.c:26-38,
+// material.cpp:110-147, 205-225).
+MatDev make_matdev(int type, double E, double nu, double Ka, double Sy, double Xt) {
+  MatDev d{};
+  d.type = type;
+  d.E = E;
+  d.nu = nu;
+  d.k = E / (3. * (1. - 2. * nu));
+  d.mu = E / (2. * (1. + nu));
+  d.lambda = nu * E / ((1. + nu) * (1. - 2. * nu));
+  d.Ka = (type == 1) ? Ka : -1.0;
+  d.Sy = (type == 1) ? Sy : -1.0;
+  d.Xt = (type == 2) ? Xt : -1.0;
+  d.two_mu = 2 * d.mu;
+  const double sqE = std::sqrt(d.E);
+  d.xt_thr = d.Xt / sqE;
+  const double Ey = 10.0e4, inf_Ey = 10. * Ey, H0 = 10.0;
+  d.dmg_r0 = Ey / sqE;
+  d.dmg_q0 = d.dmg_r0;
+  d.dmg_q1 = inf_Ey / sqE;
+  d.dmg_r1 = d.dmg_r0 + (d.dmg_q1 - d.dmg_q0) / H0;
+  d.pl_den = 2. * d.mu * (1. + d.Ka / (3. * d.mu));
+  return d;
+}
+
 void Engine::build_materials(const micropp3_config &cfg) {
   for (int i = 0; i < 3; ++i) {
     const material_base &b = cfg.materials[i];
-    MatDev &d = mats_.m[i];
     if (b.type < 0 || b.type > 2) throw std::invalid_argument("material type must be 0, 1 or 2");
-    d.type = b.type;
-    d.E = b.E;
-    d.nu = b.nu;
-    d.k = b.E / (3. * (1. - 2. * b.nu));
-    d.mu = b.E / (2. * (1. + b.nu));
-    d.lambda = b.nu * b.E / ((1. + b.nu) * (1. - 2. * b.nu));
-    d.Ka = (b.type == 1) ? b.Ka : -1.0;
-    d.Sy = (b.type == 1) ? b.Sy : -1.0;
-    d.Xt = (b.type == 2) ? b.Xt : -1.0;
-    d.two_mu = 2 * d.mu;
-    const double sqE = std::sqrt(d.E);
-    d.xt_thr = d.Xt / sqE;
-    const double Ey = 10.0e4, inf_Ey = 10. * Ey, H0 = 10.0;
-    d.dmg_r0 = Ey / sqE;
-    d.dmg_q0 = d.dmg_r0;
-    d.dmg_q1 = inf_Ey / sqE;
-    d.dmg_r1 = d.dmg_r0 + (d.dmg_q1 - d.dmg_q0) / H0;
-    d.pl_den = 2. * d.mu * (1. + d.Ka / (3. * d.mu));
+    mats_.m[i] = make_matdev(b.type, b.E, b.nu, b.Ka, b.Sy, b.Xt);
   }
 }
 
 // Element stiffness of an elastic phase, get_elem_mat (assembly.cpp:140-178) with the elastic ctan
 // (material.cpp:84-95).  B and wg are uniform over the mesh, so one Ke serves every element of the phase.
-void Engine::build_phase_stiffness() {
-  k0g32_.assign((size_t)3 * 8 * 576, 0.0f);
+void Engine::build_phase_stiffness() { phase_stiffness(mats_, ke_phase_, &k0g32_); }
+
+void Engine::phase_stiffness(const Mats &mats, double (*ke)[576], std::vector<float> *k0g) const {
+  if (k0g) k0g->assign((size_t)3 * 8 * 576, 0.0f);
   for (int ph = 0; ph < 3; ++ph) {
-    const MatDev &m = mats_.m[ph];
+    const MatDev &m = mats.m[ph];
     double C[36] = {0};
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) C[i * 6 + j] += m.lambda;
     for (int i = 0; i < 3; ++i) C[i * 6 + i] += 2 * m.mu;
     for (int i = 3; i < 6; ++i) C[i * 6 + i] = m.mu;
-    double *K = ke_phase_[ph];
+    double *K = ke[ph];
     std::memset(K, 0, 576 * sizeof(double));
     for (int gp = 0; gp < 8; ++gp) {
       double cxb[6][24];
@@ -328,7 +319,8 @@ void Engine::build_phase_stiffness() {
             Kg[i * 24 + j] += bmi * cxb[mm][j];
           }
         }
-      for (int q = 0; q < 576; ++q) k0g32_[((size_t)ph * 8 + gp) * 576 + q] = (float)Kg[q];
+      if (k0g)
+        for (int q = 0; q < 576; ++q) (*k0g)[((size_t)ph * 8 + gp) * 576 + q] = (float)Kg[q];
     }
   }
 }

@@ -50,6 +50,28 @@ struct Slot {
   InstOut *out = nullptr;
 };
 
+// Constants of one material for the device laws (engine.cpp).
+MatDev make_matdev(int type, double E, double nu, double Ka, double Sy, double Xt);
+
+// A load path of one RVE for reverse-mode gradients (path.cpp): the materials it runs with, the checkpoints
+// of its forward pass and the buffers of the adjoint pass.
+struct PathState {
+  int nsteps = 0, every = 1;
+  std::vector<double> strains;           // nsteps x 6
+  Mats mats{};
+  double ke[3][576];
+  double *d_ke = nullptr;                // per-phase elastic element matrices of `mats`
+  std::vector<double *> ck_u, ck_h;      // (u, history) before step c * every
+  std::vector<double *> seg_u, seg_h;    // a recomputed segment: u after step, history before step
+  double *h_a = nullptr, *h_b = nullptr, *mu_a = nullptr, *mu_b = nullptr;
+  AdjDev adj{};                          // BiCGSTAB vectors (x = the adjoint solution)
+  BicgState *d_st = nullptr;
+  double *d_out = nullptr;               // 21 sums of one backward step
+  bool ready = false;
+  int bicg_its = 0;                      // BiCGSTAB iterations of the last backward pass
+  bool bicg_converged = true;
+};
+
 struct NewtonResult {
   int its = 0, solver_its = 0;
   bool converged = false;
@@ -100,6 +122,13 @@ class Engine {
   void output_vtu(int gp, const char *filename);
   void print_info() const;
 
+  // Load path from the undeformed state with per-phase parameters (E, nu, Xt, Sy, Ka); checkpoints every
+  // `every` steps.  Returns 0, or 1 when a step's Newton did not converge.
+  int path_forward(int nsteps, const double *strains, const double *params, int every, double *sigma);
+  // Reverse pass of the last path: dL/dparams (3 x 5) and dL/dstrain_n (nsteps x 6, may be NULL) for
+  // L = sum_n gsigma_n . sigma_n.  Returns 0, or 1 when an adjoint solve did not converge.
+  int path_vjp(const double *gsigma, double *grad_params, double *grad_strains);
+
   double last_homogenize_ms() const { return last_ms_; }
   void set_kernel_timing(bool on);
   bool kernel_stats(const std::string &family, long *launches, double *ms, double *bytes);
@@ -113,6 +142,8 @@ class Engine {
   void build_elem_types(const micropp3_config &cfg);
   void build_materials(const micropp3_config &cfg);
   void build_phase_stiffness();
+  // Element matrices of the three phases' elastic tangents (ke) and, optionally, their Gauss-point terms.
+  void phase_stiffness(const Mats &mats, double (*ke)[576], std::vector<float> *k0g) const;
   // FP32 Jacobian of the listed slots at their current u (the residual at that u was the last one made).
   void assemble32(int nlist);
   void ensure_slots(int n);
@@ -132,6 +163,11 @@ class Engine {
   std::vector<NewtonResult> newton(const std::vector<int> &slots, const std::vector<std::array<double, 6>> &strains);
   void homogenize_fe_batch(const std::vector<int> &gp_ids);
   void allocate_vars(GpState &g);
+  // path.cpp
+  void ensure_fp64_slot0();
+  bool path_step(int n, double *h_prev, double *h_next, double *sigma);
+  void path_free();
+  int bicg_solve();
   void timer_begin(KernelTimer &t, double bytes);
   void timer_end(KernelTimer &t);
   // Adds algorithmic bytes to a timer whose launches were recorded with 0 bytes.
@@ -183,6 +219,7 @@ class Engine {
   long total_cg_its_ = 0;
   long launches_ = 0;  // kernels of this library launched by the handle
   KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_, t_upd6_;
+  PathState path_;
 };
 
 }  // namespace mgb

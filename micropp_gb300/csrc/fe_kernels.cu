@@ -7,6 +7,7 @@
 
 #include "device.cuh"
 #include "launch.h"
+#include "adjoint_laws.h"
 #include "laws.cuh"
 #include "reduce.cuh"
 
@@ -246,8 +247,9 @@ __device__ __forceinline__ float *ell_values<float>(const Inst &I) {
 
 // T = double: the plain FP64 Jacobian with the reference's forward-difference tangents.  T = float: the mixed
 // form's FP32 Jacobian -- the Gauss-point tangents are formed in closed form in FP64 and rounded once; Ke is
-// accumulated in FP32.
-template <typename T>
+// accumulated in FP32.  Dual = true (T = double): the exact derivative of the stress, column by column with
+// forward-mode dual numbers (adjoint_laws.h), for the adjoint of a load path (a missing history reads as 0).
+template <typename T, bool Dual = false>
 __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mats, const int8_t *etype,
                                                               const double *dsh_g, const T *ke_phase,
                                                               const Inst *insts, const int *list, int color) {
@@ -283,10 +285,23 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
     double eps[6], C[36];
     gp_strain(&dsh[p * 24], ue[el], eps);
     const double *vg = I.vars_old ? I.vars_old + ((size_t)e * 8 + p) * kNvarGp : nullptr;
-    if constexpr (sizeof(T) == sizeof(float))
+    if constexpr (Dual) {
+      const MatDev &md = mats.m[ph];
+      const double theta[adj::kNpar] = {md.E, md.nu, md.Xt, md.Sy, md.Ka};
+      double h[7], ds[6], dh[7];
+#pragma unroll
+      for (int i = 0; i < 7; ++i) h[i] = vg ? vg[i] : 0.0;
+#pragma unroll 1
+      for (int j = 0; j < 6; ++j) {
+        adj::law_column(md.type, theta, eps, h, j, ds, dh);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) C[i * 6 + j] = ds[i];
+      }
+    } else if constexpr (sizeof(T) == sizeof(float)) {
       law_ctan_exact(mats.m[ph], eps, vg, C);  // mixed form: closed-form consistent tangent
-    else
+    } else {
       law_ctan(mats.m[ph], eps, vg, C);  // FP64 form: the reference's forward differences
+    }
 #pragma unroll
     for (int i = 0; i < 36; ++i) Cg[el][p][i] = (T)C[i];
   }
@@ -587,7 +602,7 @@ using namespace mgb;
 
 static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
-template <typename T>
+template <typename T, bool Dual = false>
 static int launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh, const T *ke_phase,
                            const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
@@ -597,8 +612,8 @@ static int launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *ety
     const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
     const int nce = ((m->nex - cx + 1) / 2) * ((m->ney - cy + 1) / 2) * ((m->nez - cz + 1) / 2);
     if (nce <= 0) continue;
-    k_elem_mat<T><<<dim3(cdiv(nce, kMatElems), nlist), kMatElems * 24, 0, s>>>(*m, *mats, etype, dsh, ke_phase,
-                                                                               insts, list, c);
+    k_elem_mat<T, Dual><<<dim3(cdiv(nce, kMatElems), nlist), kMatElems * 24, 0, s>>>(*m, *mats, etype, dsh, ke_phase,
+                                                                                     insts, list, c);
   }
   return (int)cudaGetLastError();
 }
@@ -632,9 +647,20 @@ int mgb_launch_residual(const MeshDev *m, const Mats *mats, const int8_t *etype,
   return (int)cudaGetLastError();
 }
 
+int mgb_launch_node_gather(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_node_rhs<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  return (int)cudaGetLastError();
+}
+
 int mgb_launch_assembly(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
                         const double *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   return launch_assembly<double>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
+}
+
+int mgb_launch_assembly_dual(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
+                             const double *ke_phase, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  return launch_assembly<double, true>(m, mats, etype, dsh, ke_phase, insts, list, nlist, s);
 }
 
 int mgb_launch_assembly32(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,

@@ -22,6 +22,9 @@ int mgb_launch_residual(const mgb::MeshDev *m, const mgb::Mats *mats, const int8
                         const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_assembly(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const double *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// FP64 Jacobian with the exact Gauss-point tangents (forward-mode dual numbers), for the adjoint.
+int mgb_launch_assembly_dual(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                             const double *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_evolve(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                       const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_elem_fields(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
@@ -60,6 +63,15 @@ int mgb_launch_ctan_react(const mgb::MeshDev *m, const int *bnodes, int nbn, con
                           int nlist, cudaStream_t s);
 int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+
+// Adjoint of a load path (adjoint_kernels.cu); one instance (list[0]).
+int mgb_launch_node_gather(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_adj_rhs(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                       const mgb::Inst *insts, const int *list, const mgb::AdjStep *st, cudaStream_t s);
+int mgb_launch_adj_back(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
+                        const mgb::Inst *insts, const int *list, const mgb::AdjStep *st, cudaStream_t s);
+int mgb_launch_bicg_init(const mgb::MeshDev *m, const mgb::AdjDev *A, cudaStream_t s);
+int mgb_launch_bicg_iter(const mgb::MeshDev *m, const mgb::AdjDev *A, unsigned int *active, cudaStream_t s);
 
 #ifdef __cplusplus
 }

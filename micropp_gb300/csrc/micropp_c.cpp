@@ -197,6 +197,21 @@ void micropp3_read_restart(const struct micropp3 *self, const int restart_id) {
 
 // ---- extensions -------------------------------------------------------------------------------------
 
+int micropp3_path_forward(struct micropp3 *self, int nsteps, const double *strains, const double *params,
+                          int checkpoint_every, double *sigma) {
+  int rc = -2;
+  if (Engine *e = eng(self, "micropp3_path_forward"))
+    guard("micropp3_path_forward", [&] { rc = e->path_forward(nsteps, strains, params, checkpoint_every, sigma); });
+  return rc;
+}
+
+int micropp3_path_vjp(struct micropp3 *self, const double *gsigma, double *grad_params, double *grad_strains) {
+  int rc = -2;
+  if (Engine *e = eng(self, "micropp3_path_vjp"))
+    guard("micropp3_path_vjp", [&] { rc = e->path_vjp(gsigma, grad_params, grad_strains); });
+  return rc;
+}
+
 void micropp3_homogenize_many(struct micropp3 *const *handles, int n) {
   for (int i = 0; i < n; ++i) micropp3_homogenize(handles[i]);
 }
