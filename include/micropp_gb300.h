@@ -141,7 +141,8 @@ int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, cons
  * than ctan).  micropp3_path_forward runs the RVE of this handle from the undeformed state (zero history)
  * through nsteps macro strains strains[nsteps][6], accepting every step, with the per-phase material
  * parameters params[3][5] = (E, nu, Xt, Sy, Ka) in place of the handle's (phase types and all other settings
- * are the handle's; Newton is the FP64 plain form at the handle's tolerances).  It writes the average stress
+ * are the handle's; Newton is the FP64 plain form at the handle's tolerances, with the exact consistent
+ * tangent).  It writes the average stress
  * of every step to sigma[nsteps][6] and keeps the state before every checkpoint_every-th step.
  * micropp3_path_vjp then returns, for L = sum_n gsigma[n] . sigma[n], grad_params[3][5] = dL/dparams and, if
  * grad_strains is not NULL, grad_strains[nsteps][6] = dL/dstrains[n]: an adjoint solve per step on the
@@ -152,6 +153,10 @@ int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, cons
 int micropp3_path_forward(struct micropp3 *self, int nsteps, const double *strains, const double *params,
                           int checkpoint_every, double *sigma);
 int micropp3_path_vjp(struct micropp3 *self, const double *gsigma, double *grad_params, double *grad_strains);
+/* Newton record of one step of the last micropp3_path_forward: iterations, CG iterations, status (bit 0:
+ * converged, bit 1: a CG solve stopped at cg_max_its) and |b| / |b0| of the last residual. */
+void micropp3_path_newton(const struct micropp3 *self, int step, int *its, int *cg_its, int *status,
+                          double *rel_norm);
 
 /* Totals since construction: CG iterations summed over the handle's RVEs, and kernels launched. */
 long micropp3_total_cg_its(const struct micropp3 *self);

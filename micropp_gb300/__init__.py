@@ -111,6 +111,7 @@ def load():
         "micropp3_kernel_launches": (C.c_long, [H]),
         "micropp3_path_forward": (C.c_int, [H, C.c_int, dp, dp, C.c_int, dp]),
         "micropp3_path_vjp": (C.c_int, [H, dp, dp, dp]),
+        "micropp3_path_newton": (None, [H, C.c_int, ip, ip, ip, dp]),
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
         "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                              C.c_int, ip, C.c_void_p]),
@@ -317,6 +318,12 @@ class Micropp:
         sig = np.zeros_like(e)
         rc = self._call("micropp3_path_forward", e.shape[0], _dp(e), _dp(p), int(checkpoint_every), _dp(sig))
         return sig, rc
+
+    def path_newton(self, step):
+        """(Newton its, CG its, status bits, |b|/|b0|) of a step of the last path."""
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        self._call("micropp3_path_newton", step, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+        return a.value, b.value, c.value, d.value
 
     def path_vjp(self, gsigma):
         """dL/dparams (3, 5) and dL/dstrains (nsteps, 6) for L = sum gsigma . sigma of the last path."""

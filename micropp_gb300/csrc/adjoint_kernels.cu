@@ -192,22 +192,51 @@ __global__ void __launch_bounds__(kElemBlock) k_adj_back(MeshDev m, Mats mats, c
     for (int q = 0; q < 21; ++q) st.out[q] = tot[q];
 }
 
-// ---------------------------------------------------------------------------------------------------
-// BiCGSTAB on K^T (interior rows; Dirichlet rows are identity rows and stay zero), Jacobi preconditioner.
+// u += deps . X at every node (the affine field of a macro strain increment, engineering shear): the
+// predictor of a path step, so that Newton starts from the previous solution moved with the increment.
+__global__ void __launch_bounds__(kNodeBlock) k_affine_add(MeshDev m, double *u, Voigt6 de) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const int i = n % m.nx, j = (n / m.nx) % m.ny, k = n / m.nxny;
+  const double x[3] = {i * m.dx, j * m.dy, k * m.dz};
+  const double e[3][3] = {{de.v[0], 0.5 * de.v[3], 0.5 * de.v[4]},
+                          {0.5 * de.v[3], de.v[1], 0.5 * de.v[5]},
+                          {0.5 * de.v[4], 0.5 * de.v[5], de.v[2]}};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[n * 3 + a] += e[a][0] * x[0] + e[a][1] * x[1] + e[a][2] * x[2];
+}
 
-// (K^T x)_n: the block of K^T at (n, m) is the transpose of K's block at (m, n), stored in row m at the
-// mirrored stencil slot 26 - s.
-__device__ __forceinline__ void spmv_t_node(const MeshDev &m, const double *__restrict__ vals,
-                                            const double *__restrict__ x, int n, double y[3]) {
+// x += a y over n entries (the step length of the path's line search).
+__global__ void k_axpy(int n, double *x, const double *y, double a) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) x[t] += a * y[t];
+}
+
+// ---------------------------------------------------------------------------------------------------
+// BiCGSTAB on K or K^T (interior rows; Dirichlet rows are identity rows and stay zero), Jacobi preconditioner:
+// the path's Newton corrections (K) and its adjoint systems (K^T); the reference's J2 tangent is not symmetric.
+
+// (K x)_n, or (K^T x)_n when Transpose: the block of K^T at (n, m) is the transpose of K's block at (m, n),
+// stored in row m at the mirrored stencil slot 26 - s.
+template <bool Transpose>
+__device__ __forceinline__ void spmv_node(const MeshDev &m, const double *__restrict__ vals,
+                                          const double *__restrict__ x, int n, double y[3]) {
   y[0] = y[1] = y[2] = 0.0;
   const size_t np = m.np;
 #pragma unroll 1
   for (int s = 0; s < 27; ++s) {
     const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
-    const double *v = vals + (size_t)((26 - s) * 9) * np + nb;
     const double x0 = x[nb * 3], x1 = x[nb * 3 + 1], x2 = x[nb * 3 + 2];
+    if (Transpose) {
+      const double *v = vals + (size_t)((26 - s) * 9) * np + nb;
 #pragma unroll
-    for (int fi = 0; fi < 3; ++fi) y[fi] += v[(0 * 3 + fi) * np] * x0 + v[(1 * 3 + fi) * np] * x1 + v[(2 * 3 + fi) * np] * x2;
+      for (int fi = 0; fi < 3; ++fi)
+        y[fi] += v[(0 * 3 + fi) * np] * x0 + v[(1 * 3 + fi) * np] * x1 + v[(2 * 3 + fi) * np] * x2;
+    } else {
+      const double *v = vals + (size_t)(s * 9) * np + n;
+#pragma unroll
+      for (int fi = 0; fi < 3; ++fi)
+        y[fi] += v[(fi * 3 + 0) * np] * x0 + v[(fi * 3 + 1) * np] * x1 + v[(fi * 3 + 2) * np] * x2;
+    }
   }
 }
 
@@ -254,7 +283,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_bicg_p(MeshDev m, AdjDev A) {
   }
 }
 
-// v = K^T y; alpha = rho / (rh . v)
+// v = K y (K^T y); alpha = rho / (rh . v)
+template <bool Transpose>
 __global__ void __launch_bounds__(kNodeBlock) k_bicg_v(MeshDev m, AdjDev A) {
   const BicgState *s = A.st;
   if (s->done) return;
@@ -266,7 +296,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_bicg_v(MeshDev m, AdjDev A) {
     if (bnd(m, n, i, j, k)) {
       y[0] = A.y[n * 3]; y[1] = A.y[n * 3 + 1]; y[2] = A.y[n * 3 + 2];
     } else {
-      spmv_t_node(m, A.vals, A.y, n, y);
+      spmv_node<Transpose>(m, A.vals, A.y, n, y);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -295,7 +325,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_bicg_s(MeshDev m, AdjDev A) {
   }
 }
 
-// t = K^T z; omega = (t . s) / (t . t)
+// t = K z (K^T z); omega = (t . s) / (t . t)
+template <bool Transpose>
 __global__ void __launch_bounds__(kNodeBlock) k_bicg_t(MeshDev m, AdjDev A) {
   const BicgState *s = A.st;
   if (s->done) return;
@@ -307,7 +338,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_bicg_t(MeshDev m, AdjDev A) {
     if (bnd(m, n, i, j, k)) {
       t[0] = A.z[n * 3]; t[1] = A.z[n * 3 + 1]; t[2] = A.z[n * 3 + 2];
     } else {
-      spmv_t_node(m, A.vals, A.z, n, t);
+      spmv_node<Transpose>(m, A.vals, A.z, n, t);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -371,18 +402,37 @@ int mgb_launch_adj_back(const MeshDev *m, const Mats *mats, const int8_t *etype,
   return (int)cudaGetLastError();
 }
 
+int mgb_launch_affine_add(const MeshDev *m, double *u, const double *deps, cudaStream_t s) {
+  Voigt6 de;
+  for (int q = 0; q < 6; ++q) de.v[q] = deps[q];
+  k_affine_add<<<cdiv(m->nn, kNodeBlock), kNodeBlock, 0, s>>>(*m, u, de);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_axpy(int n, double *x, const double *y, double a, cudaStream_t s) {
+  k_axpy<<<cdiv(n, 4 * kNodeBlock), kNodeBlock, 0, s>>>(n, x, y, a);
+  return (int)cudaGetLastError();
+}
+
 int mgb_launch_bicg_init(const MeshDev *m, const AdjDev *A, cudaStream_t s) {
   k_bicg_init<<<cdiv(m->nn, kNodeBlock), kNodeBlock, 0, s>>>(*m, *A);
   return (int)cudaGetLastError();
 }
 
-// One BiCGSTAB iteration (5 launches); `active` receives +1 while the solve is still iterating.
-int mgb_launch_bicg_iter(const MeshDev *m, const AdjDev *A, unsigned int *active, cudaStream_t s) {
+// One BiCGSTAB iteration (5 launches) on K (transpose = 0) or K^T; `active` receives +1 while the solve is
+// still iterating.
+int mgb_launch_bicg_iter(const MeshDev *m, const AdjDev *A, unsigned int *active, int transpose, cudaStream_t s) {
   const unsigned gr = cdiv((size_t)3 * m->nn, 4 * kNodeBlock), gn = cdiv(m->nn, kNodeBlock);
   k_bicg_p<<<gr, kNodeBlock, 0, s>>>(*m, *A);
-  k_bicg_v<<<gn, kNodeBlock, 0, s>>>(*m, *A);
+  if (transpose)
+    k_bicg_v<true><<<gn, kNodeBlock, 0, s>>>(*m, *A);
+  else
+    k_bicg_v<false><<<gn, kNodeBlock, 0, s>>>(*m, *A);
   k_bicg_s<<<gr, kNodeBlock, 0, s>>>(*m, *A);
-  k_bicg_t<<<gn, kNodeBlock, 0, s>>>(*m, *A);
+  if (transpose)
+    k_bicg_t<true><<<gn, kNodeBlock, 0, s>>>(*m, *A);
+  else
+    k_bicg_t<false><<<gn, kNodeBlock, 0, s>>>(*m, *A);
   k_bicg_r<<<gr, kNodeBlock, 0, s>>>(*m, *A, active);
   return (int)cudaGetLastError();
 }

@@ -108,6 +108,10 @@ struct Inst {
   int pad;
 };
 
+struct Voigt6 {
+  double v[6];
+};
+
 // Scalars of one BiCGSTAB solve (the adjoint system), resident on the device.
 struct BicgState {
   double rho, rho_old, alpha, omega, beta, r0, rnorm, rel_tol;

@@ -823,13 +823,18 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     if (active.empty()) break;
     upload_list(active);
     const int na = (int)active.size();
+    int bicg_its = 0;
     if (mixed) {
       assemble32(na);
     } else {
       timer_begin(t_asm_, (double)na * (8.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
       launches_ += 9;
-      check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, na, stream_),
-                   "assembly");
+      if (exact_tangent_)  // load paths: the exact consistent tangent (quadratic Newton)
+        check_launch(mgb_launch_assembly_dual(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, na, stream_),
+                     "assembly");
+      else
+        check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, na, stream_),
+                     "assembly");
       timer_end(t_asm_);
     }
     launches_ += 1;
@@ -845,6 +850,35 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
       }
       cg_solve32(active, eta);
       check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+    } else if (exact_tangent_) {
+      // A load path (slot 0 alone): BiCGSTAB on the non-symmetric exact tangent, then a backtracking line
+      // search on |b| (Armijo, step halved up to 8 times): J2 points crossing the yield surface make the
+      // full Newton step cycle on fine meshes.
+      const int s0 = active[0];
+      Slot &w = slots_[s0];
+      bicg_its = bicg_solve(false, w.du);
+      const double nb0 = norm[idx[0]];
+      double t = 1.0, best_t = 1.0, best = -1.0;
+      launches_ += 1;
+      check_launch(mgb_launch_axpy(nndim(), w.u, w.du, 1.0, stream_), "u += du");
+      for (int ls = 0; ls <= 8; ++ls) {
+        residual(active);
+        download_out();
+        const double nb = h_out_[s0].norm;
+        if (best < 0 || nb < best) {
+          best = nb;
+          best_t = t;
+        }
+        if (nb <= (1.0 - 1e-4 * t) * nb0 || !std::isfinite(nb)) break;
+        if (ls == 8) break;
+        launches_ += 1;
+        check_launch(mgb_launch_axpy(nndim(), w.u, w.du, -0.5 * t, stream_), "line search");
+        t *= 0.5;
+      }
+      if (best_t != t) {
+        launches_ += 1;
+        check_launch(mgb_launch_axpy(nndim(), w.u, w.du, best_t - t, stream_), "line search");
+      }
     } else {
       cg_solve(active);
       check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
@@ -854,13 +888,15 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     for (size_t a = 0; a < active.size(); ++a) {
       const int i = idx[a];
       const InstOut &o = h_out_[slots[i]];
-      res[i].solver_its += o.cg_its;
-      res[i].cg_maxed |= o.cg_maxed != 0;
-      total_cg_its_ += o.cg_its;
+      const int its = (exact_tangent_ && !mixed) ? bicg_its : o.cg_its;
+      res[i].solver_its += its;
+      res[i].cg_maxed |= (exact_tangent_ && !mixed) ? !last_bicg_converged_ : o.cg_maxed != 0;
+      total_cg_its_ += its;
       res[i].its++;
       norm[i] = o.norm;
     }
   }
+  for (int i = 0; i < n; ++i) res[i].rel_norm = (norm0[i] > 0) ? norm[i] / norm0[i] : 0.0;
   return res;
 }
 

@@ -70,12 +70,15 @@ struct PathState {
   bool ready = false;
   int bicg_its = 0;                      // BiCGSTAB iterations of the last backward pass
   bool bicg_converged = true;
+  std::vector<int> nr_its, cg_its, nr_conv, cg_maxed;  // per step of the forward pass
+  std::vector<double> nr_norm;           // |b| / |b0| at the end of each step's Newton
 };
 
 struct NewtonResult {
   int its = 0, solver_its = 0;
   bool converged = false;
   bool cg_maxed = false;  // some CG solve of this Newton run stopped at cg_max_its
+  double rel_norm = 0.0;  // |b| / |b0| of the last residual
 };
 
 struct KernelTimer {
@@ -128,6 +131,8 @@ class Engine {
   // Reverse pass of the last path: dL/dparams (3 x 5) and dL/dstrain_n (nsteps x 6, may be NULL) for
   // L = sum_n gsigma_n . sigma_n.  Returns 0, or 1 when an adjoint solve did not converge.
   int path_vjp(const double *gsigma, double *grad_params, double *grad_strains);
+  // Newton record of step `step` of the last path's forward pass.
+  void path_newton(int step, int *its, int *cg_its, int *converged, double *rel_norm) const;
 
   double last_homogenize_ms() const { return last_ms_; }
   void set_kernel_timing(bool on);
@@ -165,9 +170,10 @@ class Engine {
   void allocate_vars(GpState &g);
   // path.cpp
   void ensure_fp64_slot0();
-  bool path_step(int n, double *h_prev, double *h_next, double *sigma);
+  bool path_step(int n, double *h_prev, double *h_next, double *sigma, bool record);
   void path_free();
-  int bicg_solve();
+  void path_alloc_adj();
+  int bicg_solve(bool transpose, double *x);
   void timer_begin(KernelTimer &t, double bytes);
   void timer_end(KernelTimer &t);
   // Adds algorithmic bytes to a timer whose launches were recorded with 0 bytes.
@@ -188,6 +194,8 @@ class Engine {
   bool lin_stress_ = true, subiterations_ = false, calc_ctan_lin_ = true;
   int nsubiterations_ = 10;
   int precision_ = 0, ctan_mode_ = 0;
+  bool exact_tangent_ = false;  // FP64 Newton with the exact tangent and BiCGSTAB corrections (paths, slot 0)
+  bool last_bicg_converged_ = true;
 
   MeshDev mesh_{};
   Mats mats_{};

@@ -70,8 +70,11 @@ int mgb_launch_adj_rhs(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_
                        const mgb::Inst *insts, const int *list, const mgb::AdjStep *st, cudaStream_t s);
 int mgb_launch_adj_back(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, const mgb::AdjStep *st, cudaStream_t s);
+int mgb_launch_affine_add(const mgb::MeshDev *m, double *u, const double *deps, cudaStream_t s);
+int mgb_launch_axpy(int n, double *x, const double *y, double a, cudaStream_t s);
 int mgb_launch_bicg_init(const mgb::MeshDev *m, const mgb::AdjDev *A, cudaStream_t s);
-int mgb_launch_bicg_iter(const mgb::MeshDev *m, const mgb::AdjDev *A, unsigned int *active, cudaStream_t s);
+int mgb_launch_bicg_iter(const mgb::MeshDev *m, const mgb::AdjDev *A, unsigned int *active, int transpose,
+                         cudaStream_t s);
 
 #ifdef __cplusplus
 }

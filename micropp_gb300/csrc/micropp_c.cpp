@@ -212,6 +212,12 @@ int micropp3_path_vjp(struct micropp3 *self, const double *gsigma, double *grad_
   return rc;
 }
 
+void micropp3_path_newton(const struct micropp3 *self, int step, int *its, int *cg_its, int *status,
+                          double *rel_norm) {
+  if (Engine *e = eng(self, "micropp3_path_newton"))
+    guard("micropp3_path_newton", [&] { e->path_newton(step, its, cg_its, status, rel_norm); });
+}
+
 void micropp3_homogenize_many(struct micropp3 *const *handles, int n) {
   for (int i = 0; i < n; ++i) micropp3_homogenize(handles[i]);
 }

@@ -1,6 +1,9 @@
 // path.cpp -- load paths of one RVE and their reverse-mode gradients (the adjoint pass, adjoint_kernels.cu).
 //
-// A path runs the FP64 Newton of the plain form from the undeformed state through nsteps macro strains,
+// A path runs the FP64 Newton of the plain form from the undeformed state through nsteps macro strains, with
+// the exact consistent tangent of the adjoint in place of the reference's forward differences and BiCGSTAB
+// in place of CG for the corrections (the reference's J2 tangent is not symmetric), and the previous solution
+// moved with the affine field of the strain increment as the start of each step's Newton,
 // accepting every step (history h_n = H(u_n, h_{n-1}) at every Gauss point, the history present from the
 // first step on), with per-phase parameters theta = (E, nu, Xt, Sy, Ka) that replace the handle's for the
 // path only.  The forward pass keeps the state before every `every`-th step; the reverse pass recomputes each
@@ -19,7 +22,7 @@ namespace mgb {
 
 namespace {
 
-constexpr double kAdjTol = 1.0e-12;  // BiCGSTAB: ||r|| <= kAdjTol ||b||
+constexpr double kAdjTol = 1.0e-14;  // BiCGSTAB: ||r|| <= max(cg_rel_tol, kAdjTol) ||b||
 constexpr int kAdjMaxIts = 20000;
 
 }  // namespace
@@ -55,7 +58,7 @@ void Engine::path_free() {
 
 // One accepted step of the path on slot 0: Newton at strain n from the slot's current u with history h_prev,
 // then h_next = H(u, h_prev).  The stress of the step goes to sigma[6].
-bool Engine::path_step(int n, double *h_prev, double *h_next, double *sigma) {
+bool Engine::path_step(int n, double *h_prev, double *h_next, double *sigma, bool record) {
   PathState &P = path_;
   Inst &I = h_insts_[0];
   I.vars_old = h_prev;
@@ -63,36 +66,55 @@ bool Engine::path_step(int n, double *h_prev, double *h_next, double *sigma) {
   I.vars_new = h_next;
   std::array<double, 6> e;
   std::memcpy(e.data(), &P.strains[(size_t)n * 6], sizeof(e));
+  double de[6];
+  for (int q = 0; q < 6; ++q) de[q] = e[q] - (n > 0 ? P.strains[(size_t)(n - 1) * 6 + q] : 0.0);
+  launches_ += 1;
+  check_launch(mgb_launch_affine_add(&mesh_, slots_[0].u, de, stream_), "path predictor");
   const std::vector<NewtonResult> r = newton({0}, {e});
   std::memcpy(sigma, h_out_[0].sig, 6 * sizeof(double));
+  // converged also when the last allowed iteration reached the tolerance (the reference's loop tests before
+  // each iteration only)
+  const bool conv = r[0].converged || r[0].rel_norm < nr_rel_tol_ || h_out_[0].norm < nr_max_tol_;
+  if (record) {
+    P.nr_its[n] = r[0].its;
+    P.cg_its[n] = r[0].solver_its;
+    P.nr_conv[n] = conv ? 1 : 0;
+    P.cg_maxed[n] = r[0].cg_maxed ? 1 : 0;
+    P.nr_norm[n] = r[0].rel_norm;
+  }
   check(cudaMemcpyAsync(h_next, h_prev, nvars() * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "history copy");
   upload_insts();
   upload_list({0});
   launches_ += 1;
   check_launch(mgb_launch_evolve(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, 1, stream_), "path evolve");
-  return r[0].converged;
+  return conv;
 }
 
 namespace {
 
-// The handle's materials, precision and elastic element matrices swapped for the path's while a path runs.
+// The handle's materials, precision, tangent and elastic element matrices swapped for the path's while a path
+// runs (the path's Newton is FP64 with the exact consistent tangent).
 struct PathScope {
   Mats &mats;
   double *&ke;
   int &precision;
+  bool &exact;
   Mats saved_mats;
   double *saved_ke;
   int saved_precision;
-  PathScope(Mats &m, double *&k, int &p, const Mats &pm, double *pk)
-      : mats(m), ke(k), precision(p), saved_mats(m), saved_ke(k), saved_precision(p) {
+  bool saved_exact;
+  PathScope(Mats &m, double *&k, int &p, bool &x, const Mats &pm, double *pk)
+      : mats(m), ke(k), precision(p), exact(x), saved_mats(m), saved_ke(k), saved_precision(p), saved_exact(x) {
     mats = pm;
     ke = pk;
     precision = MICROPP3_FP64;
+    exact = true;
   }
   ~PathScope() {
     mats = saved_mats;
     ke = saved_ke;
     precision = saved_precision;
+    exact = saved_exact;
   }
 };
 
@@ -114,6 +136,7 @@ int Engine::path_forward(int nsteps, const double *strains, const double *params
   P.d_ke = dalloc<double>(3 * 576, "path ke");
   check(cudaMemcpy(P.d_ke, P.ke, sizeof(P.ke), cudaMemcpyHostToDevice), "path ke upload");
   ensure_fp64_slot0();
+  path_alloc_adj();
   const size_t nd = nndim(), nv = nvars();
   P.h_a = dalloc<double>(nv, "path history");
   P.h_b = dalloc<double>(nv, "path history");
@@ -124,7 +147,12 @@ int Engine::path_forward(int nsteps, const double *strains, const double *params
     P.ck_u.push_back(dalloc<double>(nd, "checkpoint u"));
     P.ck_h.push_back(dalloc<double>(nv, "checkpoint history"));
   }
-  PathScope scope(mats_, d_ke_, precision_, P.mats, P.d_ke);
+  P.nr_its.assign(nsteps, 0);
+  P.cg_its.assign(nsteps, 0);
+  P.nr_conv.assign(nsteps, 0);
+  P.cg_maxed.assign(nsteps, 0);
+  P.nr_norm.assign(nsteps, 0.0);
+  PathScope scope(mats_, d_ke_, precision_, exact_tangent_, P.mats, P.d_ke);
   bool ok = true;
   double *hp = P.h_a, *hn = P.h_b;
   for (int n = 0; n < nsteps; ++n) {
@@ -134,7 +162,7 @@ int Engine::path_forward(int nsteps, const double *strains, const double *params
       check(cudaMemcpyAsync(P.ck_h[n / every], hp, nv * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
             "checkpoint");
     }
-    ok &= path_step(n, hp, hn, sigma + (size_t)n * 6);
+    ok &= path_step(n, hp, hn, sigma + (size_t)n * 6, true);
     std::swap(hp, hn);
   }
   sync();
@@ -142,17 +170,43 @@ int Engine::path_forward(int nsteps, const double *strains, const double *params
   return ok ? 0 : 1;
 }
 
-// K^T x = b on slot 0's FP64 ELL and right-hand side; the solution in path_.adj.x.
-int Engine::bicg_solve() {
+void Engine::path_newton(int step, int *its, int *cg_its, int *converged, double *rel_norm) const {
+  const PathState &P = path_;
+  if (step < 0 || step >= (int)P.nr_its.size()) throw std::out_of_range("path_newton: no such step of the last path");
+  if (its) *its = P.nr_its[step];
+  if (cg_its) *cg_its = P.cg_its[step];
+  if (converged) *converged = P.nr_conv[step] + 2 * P.cg_maxed[step];
+  if (rel_norm) *rel_norm = P.nr_norm[step];
+}
+
+void Engine::path_alloc_adj() {
+  PathState &P = path_;
+  if (P.mu_a) return;
+  const size_t nd = nndim(), nv = nvars();
+  P.mu_a = dalloc<double>(nv, "history adjoint");
+  P.mu_b = dalloc<double>(nv, "history adjoint");
+  for (double **v : {&P.adj.x, &P.adj.r, &P.adj.rh, &P.adj.p, &P.adj.v, &P.adj.s, &P.adj.t, &P.adj.y, &P.adj.z,
+                     &P.adj.kinv})
+    *v = dalloc<double>(nd, "BiCGSTAB vector");
+  P.d_st = dalloc<BicgState>(1, "bicg state");
+  P.adj.st = P.d_st;
+  P.d_out = dalloc<double>(21, "adjoint sums");
+}
+
+// K x = b (transpose: K^T x = b) on slot 0's FP64 ELL and right-hand side, to the handle's CG tolerance.
+// Returns the iterations; last_bicg_converged_ tells whether the tolerance was met.
+int Engine::bicg_solve(bool transpose, double *x) {
   PathState &P = path_;
   Slot &w = slots_[0];
+  double *x_buf = P.adj.x;
+  P.adj.x = x;
   P.adj.b = w.b;
   P.adj.vals = w.vals;
   P.adj.red = w.red;
   P.adj.ticket = w.ticket;
   BicgState st{};
-  st.rel_tol = kAdjTol;
-  st.max_its = kAdjMaxIts;
+  st.rel_tol = std::max(cg_rel_tol_, kAdjTol);
+  st.max_its = std::min(std::max(cg_max_its_, 1), kAdjMaxIts);
   check(cudaMemcpyAsync(P.d_st, &st, sizeof(st), cudaMemcpyHostToDevice, stream_), "bicg state");
   launches_ += 1;
   check_launch(mgb_launch_bicg_init(&mesh_, &P.adj, stream_), "bicg init");
@@ -161,7 +215,7 @@ int Engine::bicg_solve() {
     check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
     for (int it = 0; it < chunk; ++it) {
       launches_ += 5;
-      check_launch(mgb_launch_bicg_iter(&mesh_, &P.adj, d_count_, stream_), "bicg iteration");
+      check_launch(mgb_launch_bicg_iter(&mesh_, &P.adj, d_count_, transpose ? 1 : 0, stream_), "bicg iteration");
     }
     check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
     sync();
@@ -169,8 +223,9 @@ int Engine::bicg_solve() {
   }
   check(cudaMemcpyAsync(&st, P.d_st, sizeof(st), cudaMemcpyDeviceToHost, stream_), "bicg state");
   sync();
-  P.bicg_its += st.its;
-  return st.converged ? 0 : 1;
+  P.adj.x = x_buf;
+  last_bicg_converged_ = st.converged != 0;
+  return st.its;
 }
 
 int Engine::path_vjp(const double *gsigma, double *grad_params, double *grad_strains) {
@@ -184,21 +239,12 @@ int Engine::path_vjp(const double *gsigma, double *grad_params, double *grad_str
       P.seg_u.push_back(dalloc<double>(nd, "segment u"));
       P.seg_h.push_back(dalloc<double>(nv, "segment history"));
     }
-  if (!P.mu_a) {
-    P.mu_a = dalloc<double>(nv, "history adjoint");
-    P.mu_b = dalloc<double>(nv, "history adjoint");
-    for (double **v : {&P.adj.x, &P.adj.r, &P.adj.rh, &P.adj.p, &P.adj.v, &P.adj.s, &P.adj.t, &P.adj.y, &P.adj.z,
-                       &P.adj.kinv})
-      *v = dalloc<double>(nd, "adjoint vector");
-    P.d_st = dalloc<BicgState>(1, "bicg state");
-    P.adj.st = P.d_st;
-    P.d_out = dalloc<double>(21, "adjoint sums");
-  }
+  path_alloc_adj();
   std::fill(grad_params, grad_params + 15, 0.0);
   if (grad_strains) std::fill(grad_strains, grad_strains + (size_t)P.nsteps * 6, 0.0);
   P.bicg_its = 0;
   P.bicg_converged = true;
-  PathScope scope(mats_, d_ke_, precision_, P.mats, P.d_ke);
+  PathScope scope(mats_, d_ke_, precision_, exact_tangent_, P.mats, P.d_ke);
   const double wgv = mesh_.wg / mesh_.vol_tot;
   const double *mu_in = nullptr;  // dL/dh after the last step: nothing depends on it
   double *mu_out = P.mu_a;
@@ -212,7 +258,7 @@ int Engine::path_vjp(const double *gsigma, double *grad_params, double *grad_str
     double *hp = P.h_a, *hn = P.h_b;
     for (int n = s0; n < s1; ++n) {
       check(cudaMemcpyAsync(P.seg_h[n - s0], hp, nv * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "segment");
-      path_step(n, hp, hn, sig.data());
+      path_step(n, hp, hn, sig.data(), false);
       check(cudaMemcpyAsync(P.seg_u[n - s0], slots_[0].u, nd * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
             "segment");
       std::swap(hp, hn);
@@ -239,7 +285,8 @@ int Engine::path_vjp(const double *gsigma, double *grad_params, double *grad_str
       launches_ += 2;
       check_launch(mgb_launch_adj_rhs(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, &st, stream_), "adjoint rhs");
       check_launch(mgb_launch_node_gather(&mesh_, d_insts_, d_list_, 1, stream_), "adjoint rhs gather");
-      if (bicg_solve() != 0) P.bicg_converged = false;
+      P.bicg_its += bicg_solve(true, P.adj.x);
+      if (!last_bicg_converged_) P.bicg_converged = false;
       launches_ += 1;
       check_launch(mgb_launch_adj_back(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, &st, stream_),
                    "adjoint step");

@@ -168,3 +168,50 @@ def test_torch_autograd_harness(gpu_lib):
     ad = float((params.grad * d).sum())
     assert abs(ad - fd) <= 1e-4 * abs(fd), (ad, fd)
     h.close()
+
+
+def test_j2_path_50cubed_20_steps_checkpoint_5(gpu_lib, capsys):
+    """The differentiation workload at full size: one 50^3 J2 RVE with 8 seeded spheres (r = 0.12, elastic),
+    a 20-step seeded cyclic strain path of amplitude 8e-3, checkpoints every 5 steps; the adjoint gradient of
+    L with respect to the matrix's E and Sy and the spheres' E against central differences (measured once for
+    all four (E, nu, yield, hardening): agreement within 2e-9 of the largest |dL/dlog theta|)."""
+    import time
+    n = 50
+    mats = [mg.material(1, 1e7, 0.3, 1e5, 1e4), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
+    h = mg.Micropp(mg.config(n, mats=mats, coupling=[mg.FE_FULL], elem_type=wl.spheres(n, 8, 0.12, seed=5),
+                             lin_stress=0, calc_ctan_lin=0, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-10,
+                             cg_rel_tol=1e-10, cg_max_its=5000))
+    rng = np.random.default_rng(11)
+    d = rng.uniform(-1, 1, 6)
+    d /= np.max(np.abs(d))
+    k = np.arange(1, 21)
+    eps = np.outer(8e-3 * np.sin(2 * np.pi * k / 10), d)  # two load cycles
+    p0 = np.array([[1e7, 0.3, 0.0, 1e4, 1e5], [1e8, 0.25, 0.0, 0.0, 0.0], [1e7, 0.25, 0.0, 0.0, 0.0]])
+    target, rc = h.path_forward(eps, p0 * 1.05, 5)
+    assert rc == 0, [h.path_newton(k) for k in range(20)]
+    t0 = time.perf_counter()
+    sig, rc = h.path_forward(eps, p0, 5)
+    t1 = time.perf_counter()
+    gp, gs, rc2 = h.path_vjp(2 * (sig - target))
+    t2 = time.perf_counter()
+    assert rc == 0 and rc2 == 0
+    checks = [(0, 0), (0, 3), (1, 0)]
+    fd = {}
+    for ph, q in checks:
+        step = 1e-5 * p0[ph, q]
+        pp, pm = p0.copy(), p0.copy()
+        pp[ph, q] += step
+        pm[ph, q] -= step
+        lp = np.sum((h.path_forward(eps, pp, 5)[0] - target) ** 2)
+        lm = np.sum((h.path_forward(eps, pm, 5)[0] - target) ** 2)
+        fd[(ph, q)] = (lp - lm) / (2 * step)
+    ref = max(abs(fd[c]) * p0[c] for c in checks)
+    with capsys.disabled():
+        print(f"\n50^3 J2, 20 steps: forward {t1 - t0:.2f} s, reverse (2 recomputed segments per checkpoint) "
+              f"{t2 - t1:.2f} s")
+        for c in checks:
+            print(f"  dL/dtheta{c}: adjoint {gp[c]:.9e}  central difference {fd[c]:.9e}  "
+                  f"rel. to max |dL/dlog theta| {abs(gp[c] - fd[c]) * p0[c] / ref:.2e}")
+    for c in checks:
+        assert abs(gp[c] - fd[c]) * p0[c] <= TOL_GRAD * ref, (c, gp[c], fd[c])
+    h.close()
