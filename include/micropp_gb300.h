@@ -107,6 +107,9 @@ double micropp3_last_homogenize_ms(const struct micropp3 *self);
  * algorithmic bytes moved by those launches.  Families: "spmv" (the Newton CG's SpMV), "cg_update" (its two
  * vector kernels), "spmv6" and "cg6_update" (the same for the 6-RHS tangent CG), "assembly", "residual". */
 void micropp3_set_kernel_timing(struct micropp3 *self, int enable);
+/* CUDA graphs: the CG iterations run in chunks captured once per (solver, batch size) and replayed
+ * (default on; chunks are launched directly while kernel timing is on). */
+void micropp3_set_cuda_graphs(struct micropp3 *self, int enable);
 int micropp3_kernel_stats(const struct micropp3 *self, const char *family, long *launches, double *ms,
                           double *bytes);
 

@@ -112,6 +112,7 @@ def load():
         "micropp3_path_forward": (C.c_int, [H, C.c_int, dp, dp, C.c_int, dp]),
         "micropp3_path_vjp": (C.c_int, [H, dp, dp, dp]),
         "micropp3_path_newton": (None, [H, C.c_int, ip, ip, ip, dp]),
+        "micropp3_set_cuda_graphs": (None, [H, C.c_int]),
         "micropp3_homogenize_many": (None, [C.POINTER(H), C.c_int]),
         "micropp3_ell_solve_cgpd": (C.c_int, [ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                              C.c_int, ip, C.c_void_p]),
@@ -318,6 +319,9 @@ class Micropp:
         sig = np.zeros_like(e)
         rc = self._call("micropp3_path_forward", e.shape[0], _dp(e), _dp(p), int(checkpoint_every), _dp(sig))
         return sig, rc
+
+    def set_cuda_graphs(self, on):
+        self._call("micropp3_set_cuda_graphs", 1 if on else 0)
 
     def path_newton(self, step):
         """(Newton its, CG its, status bits, |b|/|b0|) of a step of the last path."""

@@ -6,6 +6,7 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -160,6 +161,7 @@ Engine::~Engine() {
     dfree(g.vars_n);
     dfree(g.vars_k);
   }
+  clear_graphs();
   path_free();
   free_slots();
   for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_})
@@ -428,6 +430,7 @@ void Engine::ensure_slots(int n) {
     check(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), stream_), "ticket");
     check(cudaMemsetAsync(w.out, 0, sizeof(InstOut), stream_), "out");
   }
+  clear_graphs();  // the captured chunks hold the instance and list pointers
   dfree(d_insts_);
   d_insts_ = dalloc<Inst>(n, "insts");
   if (h_out_) cudaFreeHost(h_out_);
@@ -499,6 +502,49 @@ double Engine::listed_cg_its(const std::vector<int> &slots) {
 }
 
 void Engine::sync() { check(cudaStreamSynchronize(stream_), "stream synchronize"); }
+
+// A chunk of CG iterations (`body` launches them on stream_): replayed from a CUDA graph captured the first
+// time this (solver, batch size) pair runs, or launched directly while per-kernel timing is on or graphs are
+// off.  The kernels read the instance list and the CG states from device memory, so one capture serves every
+// later solve with the same number of listed instances.
+void Engine::run_chunk(int kind, int n, const std::function<void()> &body) {
+  const bool timing = t_spmv_.enabled || t_update_.enabled || t_spmv6_.enabled || t_upd6_.enabled;
+  if (!graphs_ || timing) {
+    body();
+    return;
+  }
+  const long key = (long)kind * 1000000L + n;
+  auto it = graph_cache_.find(key);
+  if (it == graph_cache_.end()) {
+    cudaGraph_t g = nullptr;
+    check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(stream_, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    check(cudaStreamEndCapture(stream_, &g), "graph capture end");
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    check(e, "graph instantiate");
+    it = graph_cache_.emplace(key, ex).first;
+  }
+  check(cudaGraphLaunch(it->second, stream_), "graph launch");
+}
+
+void Engine::clear_graphs() {
+  if (!graph_cache_.empty() && stream_) cudaStreamSynchronize(stream_);
+  for (auto &kv : graph_cache_) cudaGraphExecDestroy(kv.second);
+  graph_cache_.clear();
+}
+
+void Engine::set_graphs(bool on) {
+  if (!on) clear_graphs();
+  graphs_ = on;
+}
 
 void Engine::timer_begin(KernelTimer &t, double bytes) {
   if (!t.enabled) return;
@@ -601,17 +647,19 @@ void Engine::cg_solve(const std::vector<int> &slots) {
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
-    for (int it = 0; it < chunk; ++it) {
-      if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-      timer_begin(t_spmv_, 0.0);
-      launches_ += 3;
-      check_launch(mgb_launch_cg_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg spmv");
-      timer_end(t_spmv_);
-      timer_begin(t_update_, 0.0);
-      check_launch(mgb_launch_cg_update(&mesh_, d_insts_, d_list_, n, stream_), "cg update");
-      check_launch(mgb_launch_cg_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg p-update");
-      timer_end(t_update_);
-    }
+    run_chunk(0, n, [&] {
+      for (int it = 0; it < chunk; ++it) {
+        if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+        timer_begin(t_spmv_, 0.0);
+        check_launch(mgb_launch_cg_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg spmv");
+        timer_end(t_spmv_);
+        timer_begin(t_update_, 0.0);
+        check_launch(mgb_launch_cg_update(&mesh_, d_insts_, d_list_, n, stream_), "cg update");
+        check_launch(mgb_launch_cg_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg p-update");
+        timer_end(t_update_);
+      }
+    });
+    launches_ += 3 * chunk;
     done_its += chunk;
     check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
     sync();
@@ -643,17 +691,19 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   const int chunk = (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
-    for (int it = 0; it < chunk; ++it) {
-      if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-      timer_begin(t_spmv_, 0.0);
-      launches_ += 3;
-      check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg32 spmv");
-      timer_end(t_spmv_);
-      timer_begin(t_update_, 0.0);
-      check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
-      check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
-      timer_end(t_update_);
-    }
+    run_chunk(1, n, [&] {
+      for (int it = 0; it < chunk; ++it) {
+        if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+        timer_begin(t_spmv_, 0.0);
+        check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg32 spmv");
+        timer_end(t_spmv_);
+        timer_begin(t_update_, 0.0);
+        check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
+        check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
+        timer_end(t_update_);
+      }
+    });
+    launches_ += 3 * chunk;
     done_its += chunk;
     check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
     sync();
@@ -747,17 +797,19 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
     const int nl = (int)live.size();
     int done_its = 0;
     while (done_its <= cg_max_its_) {
-      for (int it = 0; it < chunk; ++it) {
-        if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
-        timer_begin(t_spmv6_, 0.0);
-        launches_ += 3;
-        check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 spmv");
-        timer_end(t_spmv6_);
-        timer_begin(t_upd6_, 0.0);
-        check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");
-        check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
-        timer_end(t_upd6_);
-      }
+      run_chunk(2, nl, [&] {
+        for (int it = 0; it < chunk; ++it) {
+          if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
+          timer_begin(t_spmv6_, 0.0);
+          check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 spmv");
+          timer_end(t_spmv6_);
+          timer_begin(t_upd6_, 0.0);
+          check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");
+          check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
+          timer_end(t_upd6_);
+        }
+      });
+      launches_ += 3 * chunk;
       done_its += chunk;
       check(cudaMemcpyAsync(h_count_, d_count_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "count");
       sync();

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -135,6 +137,8 @@ class Engine {
   void path_newton(int step, int *its, int *cg_its, int *converged, double *rel_norm) const;
 
   double last_homogenize_ms() const { return last_ms_; }
+  void set_graphs(bool on);
+  bool graphs() const { return graphs_; }
   void set_kernel_timing(bool on);
   bool kernel_stats(const std::string &family, long *launches, double *ms, double *bytes);
   long total_cg_its() const { return total_cg_its_; }
@@ -173,6 +177,8 @@ class Engine {
   bool path_step(int n, double *h_prev, double *h_next, double *sigma, bool record);
   void path_free();
   void path_alloc_adj();
+  void run_chunk(int kind, int n, const std::function<void()> &body);
+  void clear_graphs();
   int bicg_solve(bool transpose, double *x);
   void timer_begin(KernelTimer &t, double bytes);
   void timer_end(KernelTimer &t);
@@ -228,6 +234,8 @@ class Engine {
   long launches_ = 0;  // kernels of this library launched by the handle
   KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_, t_upd6_;
   PathState path_;
+  bool graphs_ = true;                         // CG chunks replayed from captured CUDA graphs
+  std::map<long, cudaGraphExec_t> graph_cache_;  // (solver, listed instances) -> executable graph
 };
 
 }  // namespace mgb

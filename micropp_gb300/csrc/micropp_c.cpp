@@ -218,6 +218,10 @@ void micropp3_path_newton(const struct micropp3 *self, int step, int *its, int *
     guard("micropp3_path_newton", [&] { e->path_newton(step, its, cg_its, status, rel_norm); });
 }
 
+void micropp3_set_cuda_graphs(struct micropp3 *self, int enable) {
+  if (Engine *e = eng(self, "micropp3_set_cuda_graphs")) guard("micropp3_set_cuda_graphs", [&] { e->set_graphs(enable != 0); });
+}
+
 void micropp3_homogenize_many(struct micropp3 *const *handles, int n) {
   for (int i = 0; i < n; ++i) micropp3_homogenize(handles[i]);
 }
