@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--cpu-sample-rves", type=int, default=0, help="RVEs in the CPU sample (default: host cores)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--forms", default="fast,plain", help="forms to measure; the first is the headline value")
+    p.add_argument("--workload", default="rve60", choices=["rve60", "mixed"],
+                   help="rve60: the headline (R damage RVEs of --size^3); mixed: 256 RVEs of mixed sizes, "
+                        "microstructures and laws, 5 increments (not the headline)")
+    p.add_argument("--mixed-rves", type=int, default=256)
     return p.parse_args()
 
 
@@ -472,10 +476,86 @@ def run_gpu(args):
     print(json.dumps(line))
 
 
+def run_mixed(args):
+    """256 RVEs of uneven size drawn from {20,30,40,50,60}^3, each a centred sphere (r = 0.2) or 4 layers normal
+    to z, with an elastic, damage or J2 matrix; every RVE is taken through 5 increments to a seeded strain
+    target (~U[-5e-3, 5e-3], damage ~U[-2.5e-2, 2.5e-2] so that it loads).  RVEs that share size,
+    microstructure and law are Gauss points of one handle (one batch), and micropp3_homogenize_many runs the
+    handles concurrently.  Value: stress + ctan homogenizations/s over the 5 increments (wall clock)."""
+    import ctypes
+
+    import micropp_gb300 as mg
+    from micropp_gb300 import build
+    from micropp_gb300 import workloads as wl
+    build.build()
+    L = mg.load()
+    rng = np.random.default_rng(args.seed)
+    R = args.mixed_rves
+    sizes = rng.choice([20, 30, 40, 50, 60], size=R)
+    micro = rng.integers(0, 2, R)
+    law = rng.integers(0, 3, R)
+    groups = {}
+    for i in range(R):
+        groups.setdefault((int(sizes[i]), int(micro[i]), int(law[i])), []).append(i)
+    targets = np.zeros((R, 6))
+    for i in range(R):
+        targets[i] = rng.uniform(-1, 1, 6) * (2.5e-2 if law[i] == 1 else 5e-3)
+    lawmat = {0: mg.material(0, 1e7, 0.25), 1: mg.material(2, 1e7, 0.25, 0, 0, 1e5),
+              2: mg.material(1, 1e7, 0.3, 1e5, 1e4)}
+    out = []
+    for form in [f for f in args.forms.split(",") if f in FORMS and f != "plain_batched"]:
+        handles, members = [], []
+        for (n, mi, lw), idx in sorted(groups.items()):
+            mats = [lawmat[lw], mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
+            kw = dict(FORMS[form]["cfg"])
+            et = wl.layers_z(n) if mi == 1 else None
+            cfg = mg.config(n, ngp=len(idx), micro_type=mg.MIC_SPHERE if mi == 0 else mg.MIC_HOMOGENEOUS,
+                            geo=(0.2, 0.1, 0.1, 0.1), mats=mats, coupling=[2] * len(idx), elem_type=et, lin_stress=0,
+                            calc_ctan_lin=0, **kw)
+            handles.append(mg.Micropp(cfg))
+            members.append(idx)
+        arr = (ctypes.POINTER(mg.Handle) * len(handles))(*[ctypes.pointer(h.h) for h in handles])
+
+        def set_inc(k):
+            for h, idx in zip(handles, members):
+                for gp, i in enumerate(idx):
+                    h.set_strain(gp, targets[i] * k / 5.0)
+        set_inc(1)
+        L.micropp3_homogenize_many(arr, len(handles))  # warm-up: workspace, graphs (state not accepted)
+        cg0 = sum(h.total_cg_its() for h in handles)
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            for k in range(1, 6):
+                set_inc(k)
+                L.micropp3_homogenize_many(arr, len(handles))
+                for h in handles:
+                    h.update_vars()
+            wall = time.perf_counter() - t0
+        if L.micropp3_last_error():
+            raise RuntimeError(L.micropp3_last_error().decode())
+        cg = sum(h.total_cg_its() for h in handles) - cg0
+        status = [h.status(gp) for h, idx in zip(handles, members) for gp in range(len(idx))]
+        out.append({"form": form, "value": 5 * R / wall, "wall_s": wall, "cg_its": cg, "handles": len(handles),
+                    "status_counts": {str(k): status.count(k) for k in sorted(set(status))}, "clocks": clk.summary()})
+        for h in handles:
+            h.close()
+    head = out[0]
+    print(json.dumps({
+        "metric": "RVE homogenizations/s (stress+ctan), 256 RVEs of mixed sizes, microstructures and laws, 1 GB300",
+        "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": 5, "warmup": 1,
+        "ms_per_step": 1e3 * head["wall_s"] / 5, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if FORMS[head["form"]]["cfg"]["precision"] == 1 else "f64", "data": "synthetic",
+        "config": {"workload": f"{R} RVEs, sizes {{20..60}}^3, sphere or layers, elastic/damage/J2, 5 increments",
+                   "groups": len(groups), "form": head["form"]},
+        "forms": {o["form"]: {k: v for k, v in o.items() if k != "form"} for o in out}}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "mixed":
+        run_mixed(args)
     else:
         run_gpu(args)
 

@@ -79,7 +79,9 @@ void micropp3_new_ext(struct micropp3 *self, const struct micropp3_config *cfg);
 const char *micropp3_last_error(void);
 void micropp3_clear_error(void);
 
-/* Homogenize several handles in one batched pass (RVEs of different sizes and materials). */
+/* Homogenize several handles at once (RVEs of different sizes, microstructures or materials): each handle's
+ * Gauss points form one batch on the handle's own stream, and the handles run concurrently from worker
+ * threads.  Do not use the handles from another thread meanwhile. */
 void micropp3_homogenize_many(struct micropp3 *const *handles, int n);
 
 /* Status word (MICROPP3_STATUS_*) of macro point gp after the last homogenize(). */

@@ -3,10 +3,14 @@
 // Each entry forwards to the handle's Engine like the reference wrapper (micropp_c.cpp:29-142).  Failures
 // (a bad argument, a CUDA error) cannot surface through the reference's void signatures, so they are
 // printed on stderr and kept for micropp3_last_error(); a failed micropp3_new leaves self->ptr NULL.
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <exception>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "engine.hpp"
 #include "micropp_c.h"
@@ -223,7 +227,34 @@ void micropp3_set_cuda_graphs(struct micropp3 *self, int enable) {
 }
 
 void micropp3_homogenize_many(struct micropp3 *const *handles, int n) {
-  for (int i = 0; i < n; ++i) micropp3_homogenize(handles[i]);
+  if (n <= 0) return;
+  if (!handles) {
+    fail("micropp3_homogenize_many", "handles is NULL");
+    return;
+  }
+  std::vector<Engine *> engines(n);
+  for (int i = 0; i < n; ++i)
+    if (!(engines[i] = eng(handles[i], "micropp3_homogenize_many"))) return;
+  // Every handle has its own stream: homogenize them from worker threads so that their batches (RVEs of
+  // different sizes or materials) run on the GPU at the same time.
+  std::vector<std::string> errors(n);
+  std::atomic<int> next(0);
+  auto work = [&] {
+    for (int i; (i = next.fetch_add(1)) < n;) {
+      try {
+        engines[i]->homogenize();
+      } catch (const std::exception &e) {
+        errors[i] = e.what();
+      }
+    }
+  };
+  const int nthreads = std::min(n, 16);
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);
+  work();
+  for (auto &t : pool) t.join();
+  for (int i = 0; i < n; ++i)
+    if (!errors[i].empty()) fail("micropp3_homogenize_many", ("handle " + std::to_string(i) + ": " + errors[i]).c_str());
 }
 
 int micropp3_get_status(const struct micropp3 *self, int gp_id) {
