@@ -855,6 +855,20 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
   residual(slots);
   download_out();
   for (int i = 0; i < n; ++i) norm0[i] = norm[i] = h_out_[slots[i]].norm;
+  if (!predict_de_.empty()) {
+    // Predictor (mixed form): |b0| stays the residual at u_n with the new boundary values, as in the reference,
+    // so nr_rel_tol keeps its meaning; Newton then starts from u_n + deps . X (boundary values unchanged).
+    for (int i = 0; i < n; ++i) {
+      launches_ += 1;
+      check_launch(mgb_launch_affine_add(&mesh_, slots_[slots[i]].u, predict_de_[i].data(), stream_), "predictor");
+    }
+    predict_de_.clear();
+    launches_ += 1;
+    check_launch(mgb_launch_set_bc(&mesh_, d_insts_, d_list_, n, stream_), "set_bc");
+    residual(slots);
+    download_out();
+    for (int i = 0; i < n; ++i) norm[i] = h_out_[slots[i]].norm;
+  }
   while (true) {
     std::vector<int> active;
     std::vector<int> idx;
@@ -876,6 +890,7 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     upload_list(active);
     const int na = (int)active.size();
     int bicg_its = 0;
+    bool have_residual = false;
     if (mixed) {
       assemble32(na);
     } else {
@@ -901,7 +916,33 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
         eta[a] = std::max(cg_rel_tol_, std::min(0.1, want));
       }
       cg_solve32(active, eta);
+      launches_ += 1;
       check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+      residual(active);
+      download_out();
+      have_residual = true;
+      // Backtracking line search per instance (Armijo on |b|, step halved up to 8 times): a full step that
+      // does not reduce the residual (J2 points crossing the yield surface) is shortened.
+      std::vector<double> t(na, 1.0);
+      for (int ls = 0; ls < 8; ++ls) {
+        std::vector<int> back;
+        for (int a = 0; a < na; ++a) {
+          const double nb = h_out_[active[a]].norm;
+          if (std::isfinite(nb) && nb > (1.0 - 1e-4 * t[a]) * norm[idx[a]]) back.push_back(a);
+        }
+        if (back.empty()) break;
+        std::vector<int> bslots;
+        for (int a : back) {
+          launches_ += 1;
+          check_launch(mgb_launch_axpy_du32(&mesh_, slots_[active[a]].u, slots_[active[a]].du32, -0.5 * t[a], stream_),
+                       "line search");
+          t[a] *= 0.5;
+          bslots.push_back(active[a]);
+        }
+        upload_list(bslots);
+        residual(bslots);
+        download_out();
+      }
     } else if (exact_tangent_) {
       // A load path (slot 0 alone): BiCGSTAB on the non-symmetric exact tangent, then a backtracking line
       // search on |b| (Armijo, step halved up to 8 times): J2 points crossing the yield surface make the
@@ -935,8 +976,10 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
       cg_solve(active);
       check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
     }
-    residual(active);
-    download_out();
+    if (!have_residual) {
+      residual(active);
+      download_out();
+    }
     for (size_t a = 0; a < active.size(); ++a) {
       const int i = idx[a];
       const InstOut &o = h_out_[slots[i]];
@@ -982,6 +1025,14 @@ void Engine::homogenize_fe_batch(const std::vector<int> &gp_ids) {
     g.subiterated = false;
     g.status = 0;
     std::memcpy(strains[i].data(), g.strain, sizeof(g.strain));
+  }
+  if (precision_ == MICROPP3_MIXED) {
+    // the mixed form's Newton starts from u_n moved with the affine field of the strain increment
+    predict_de_.resize(n);
+    for (int i = 0; i < n; ++i) {
+      const GpState &g = gps_[gp_ids[i]];
+      for (int v = 0; v < 6; ++v) predict_de_[i][v] = g.strain[v] - g.strain_old[v];
+    }
   }
   std::vector<NewtonResult> r = newton(all, strains);
   std::vector<int> last_sits(n);

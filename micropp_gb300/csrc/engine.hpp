@@ -202,6 +202,7 @@ class Engine {
   int precision_ = 0, ctan_mode_ = 0;
   bool exact_tangent_ = false;  // FP64 Newton with the exact tangent and BiCGSTAB corrections (paths, slot 0)
   bool last_bicg_converged_ = true;
+  std::vector<std::array<double, 6>> predict_de_;  // strain increments of the next newton() call's predictor
 
   MeshDev mesh_{};
   Mats mats_{};

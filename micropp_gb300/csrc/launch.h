@@ -48,6 +48,7 @@ int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const 
 int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                             unsigned int *active_count, cudaStream_t s);
 int mgb_launch_add_du32(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_axpy_du32(const mgb::MeshDev *m, double *u, const float *du, double a, cudaStream_t s);
 int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
                            cudaStream_t s);

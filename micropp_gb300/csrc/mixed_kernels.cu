@@ -264,6 +264,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_pupdate(MeshDev m, const In
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(active_count, 1u);
 }
 
+// u += a du32 of one instance (the step length of the mixed form's line search).
+__global__ void k_axpy_du32(int nndim, double *u, const float *du, double a) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nndim; t += gridDim.x * blockDim.x)
+    u[t] += a * (double)du[t];
+}
+
 __global__ void k_add_du32(int nndim, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   double *__restrict__ u = I.u;
@@ -810,6 +816,12 @@ int mgb_launch_add_du32(const MeshDev *m, const Inst *insts, const int *list, in
   if (nlist <= 0) return 0;
   const int nndim = m->nn * 3;
   k_add_du32<<<dim3(cdiv(nndim, 4 * kNodeBlock), nlist), kNodeBlock, 0, s>>>(nndim, insts, list);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_axpy_du32(const MeshDev *m, double *u, const float *du, double a, cudaStream_t s) {
+  const int nndim = m->nn * 3;
+  k_axpy_du32<<<cdiv(nndim, 4 * kNodeBlock), kNodeBlock, 0, s>>>(nndim, u, du, a);
   return (int)cudaGetLastError();
 }
 
