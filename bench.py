@@ -52,9 +52,12 @@ def parse():
     p.add_argument("--cpu-sample-rves", type=int, default=0, help="RVEs in the CPU sample (default: host cores)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--forms", default="fast,plain", help="forms to measure; the first is the headline value")
-    p.add_argument("--workload", default="rve60", choices=["rve60", "mixed"],
+    p.add_argument("--workload", default="rve60", choices=["rve60", "mixed", "precision"],
                    help="rve60: the headline (R damage RVEs of --size^3); mixed: 256 RVEs of mixed sizes, "
-                        "microstructures and laws, 5 increments (not the headline)")
+                        "microstructures and laws, 5 increments; precision: one J2 RVE of --precision-size^3 "
+                        "along a 20-step uniaxial path, fast form against plain FP64 (neither is the headline)")
+    p.add_argument("--precision-size", type=int, default=100)
+    p.add_argument("--precision-steps", type=int, default=20)
     p.add_argument("--mixed-rves", type=int, default=256)
     return p.parse_args()
 
@@ -550,12 +553,58 @@ def run_mixed(args):
         "forms": {o["form"]: {k: v for k, v in o.items() if k != "form"} for o in out}}))
 
 
+def run_precision(args):
+    """One RVE of n^3 elements (default 100^3, 3,090,903 DOF): J2 matrix (E = 1e7, nu = 0.3, Sy = 1e4,
+    Ka = 1e5) with 8 seeded non-overlapping elastic spheres (r = 0.12, E = 1e8, nu = 0.25), uniaxial strain
+    eps_xx to 1e-2 in 20 steps (--precision-steps), every step accepted (FE_ONE_WAY: average stress per step).  The plain FP64 form
+    (the reference algorithm, parity-tested against the oracle) and the fast form run the same path with tight
+    tolerances (Newton 1e-10 relative, CG 1e-10); reports the fast form's stress error per step relative to the
+    largest stress entry, and both forms' device time."""
+    import micropp_gb300 as mg
+    from micropp_gb300 import build
+    from micropp_gb300 import workloads as wl
+    build.build()
+    n = args.precision_size
+    et = wl.spheres(n, 8, 0.12, seed=args.seed)
+    mats = [mg.material(1, 1e7, 0.3, 1e5, 1e4), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
+    tight = dict(coupling=[1], elem_type=et, lin_stress=0, calc_ctan_lin=0, nr_max_its=30, nr_max_tol=1e-30,
+                 nr_rel_tol=1e-10, cg_rel_tol=1e-10, cg_max_its=20000, mats=mats)
+    res = {}
+    for form, prec in (("plain", 0), ("fast", 1)):
+        h = mg.Micropp(mg.config(n, precision=prec, **tight))
+        sig, ms, its = [], 0.0, []
+        ns = args.precision_steps
+        with ClockSampler(0) as clk:
+            for k in range(1, ns + 1):
+                h.set_strain(0, [1e-2 * k / ns, 0, 0, 0, 0, 0])
+                h.homogenize()
+                ms += h.last_homogenize_ms()
+                sig.append(h.get_stress(0))
+                its.append(h.newton(0)[:2] + (h.has_converged(0),))
+                h.update_vars()
+                print(f"{form} step {k}: sigma_xx {sig[-1][0]:.9e} newton {its[-1]} {ms / 1e3:.1f} s", file=sys.stderr,
+                      flush=True)
+        res[form] = {"sigma": np.array(sig), "device_s": ms / 1e3, "newton": its, "clocks": clk.summary()}
+        h.close()
+    sp, sf = res["plain"]["sigma"], res["fast"]["sigma"]
+    err = [float(np.max(np.abs(sf[k] - sp[k])) / np.max(np.abs(sp[k]))) for k in range(len(sp))]
+    print(json.dumps({
+        "workload": f"precision: one J2 RVE of {n}^3 with 8 spheres, uniaxial eps_xx to 1e-2 in "
+                    f"{args.precision_steps} steps",
+        "dof": 3 * (n + 1) ** 3, "stress_rel_err_per_step": err, "max_stress_rel_err": max(err),
+        "plain_device_s": res["plain"]["device_s"], "fast_device_s": res["fast"]["device_s"],
+        "plain_newton": res["plain"]["newton"], "fast_newton": res["fast"]["newton"],
+        "sigma_xx_final": float(sp[-1][0]), "clocks": res["fast"]["clocks"]}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "mixed":
         run_mixed(args)
+    elif args.workload == "precision":
+        run_precision(args)
     else:
         run_gpu(args)
 
