@@ -33,6 +33,9 @@ constexpr double kTangentSweepRel = 1.0e-5;
 constexpr double kTangentTol = 1.0e-9;
 constexpr int kTangentSweeps = 4;
 
+// Lowest relative tolerance asked of the mixed form's FP32 Newton CG.
+constexpr double kFp32CgFloor = 1.0e-6;
+
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
 }  // namespace
@@ -908,12 +911,13 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     if (mixed) {
       // Inexact Newton: the FP64 residual corrects each FP32 solve, so a correction only needs to gain the
       // digits still missing to the Newton tolerance: eta = 0.05 * nr_rel_tol * |b0| / |b_k|, kept within
-      // [cg_rel_tol, 0.1].
+      // [max(cg_rel_tol, kFp32CgFloor), 0.1] (an FP32 CG cannot reduce its residual much below 1e-6).
       std::vector<double> eta(active.size());
+      const double floor = std::max(cg_rel_tol_, kFp32CgFloor);
       for (size_t a = 0; a < active.size(); ++a) {
         const int i = idx[a];
-        const double want = (norm[i] > 0) ? 0.05 * nr_rel_tol_ * norm0[i] / norm[i] : cg_rel_tol_;
-        eta[a] = std::max(cg_rel_tol_, std::min(0.1, want));
+        const double want = (norm[i] > 0) ? 0.05 * nr_rel_tol_ * norm0[i] / norm[i] : floor;
+        eta[a] = std::max(floor, std::min(0.1, want));
       }
       cg_solve32(active, eta);
       launches_ += 1;
