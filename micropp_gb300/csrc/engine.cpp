@@ -7,6 +7,9 @@
 
 #include <algorithm>
 #include <functional>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -181,6 +184,8 @@ Engine::~Engine() {
   dfree(d_bnodes_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
+  for (cudaEvent_t e : tune_ev_)
+    if (e) cudaEventDestroy(e);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -538,6 +543,52 @@ void Engine::run_chunk(int kind, int n, const std::function<void()> &body) {
   check(cudaGraphLaunch(it->second, stream_), "graph launch");
 }
 
+// Autotuner of the FP32 SpMV block sizes.  The first time a (kernel, RVE size, batch size) runs, each block
+// size is timed on the live data right after the CG set-up (3 launches each, CUDA events on the stream; an
+// SpMV launch is idempotent: same p in, same Ap and alpha out) and the fastest is kept for the process.
+namespace {
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int>, int> g_tuned;
+}  // namespace
+
+int Engine::tuned_block(int kind, int nlist) {
+  const auto key = std::make_tuple(kind, mesh_.nn, nlist);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) return it->second;
+  }
+  if (!tune_ev_[0]) {
+    check(cudaEventCreate(&tune_ev_[0]), "tune event");
+    check(cudaEventCreate(&tune_ev_[1]), "tune event");
+  }
+  int best = 128;
+  float best_ms = 0.0f;
+  for (int block : {64, 128, 256}) {
+    auto launch = [&] {
+      launches_ += 1;
+      if (kind == 0)
+        check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, nlist, block, stream_), "tune spmv");
+      else
+        check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nlist, block, stream_), "tune spmv6");
+    };
+    launch();  // warm
+    check(cudaEventRecord(tune_ev_[0], stream_), "tune event");
+    for (int r = 0; r < 3; ++r) launch();
+    check(cudaEventRecord(tune_ev_[1], stream_), "tune event");
+    check(cudaEventSynchronize(tune_ev_[1]), "tune sync");
+    float ms = 0.0f;
+    check(cudaEventElapsedTime(&ms, tune_ev_[0], tune_ev_[1]), "tune elapsed");
+    if (block == 64 || ms < best_ms) {
+      best_ms = ms;
+      best = block;
+    }
+  }
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tuned[key] = best;
+  return best;
+}
+
 void Engine::clear_graphs() {
   if (!graph_cache_.empty() && stream_) cudaStreamSynchronize(stream_);
   for (auto &kv : graph_cache_) cudaGraphExecDestroy(kv.second);
@@ -688,6 +739,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   }
   launches_ += 1;
   check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
+  const int block = tuned_block(0, n);
   const double nrow = (double)nndim();
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 4);  // per iteration and instance, as in cg_solve
   const double upd_bytes = nrow * 11.0 * 4;
@@ -698,7 +750,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
       for (int it = 0; it < chunk; ++it) {
         if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
         timer_begin(t_spmv_, 0.0);
-        check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, stream_), "cg32 spmv");
+        check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, block, stream_), "cg32 spmv");
         timer_end(t_spmv_);
         timer_begin(t_update_, 0.0);
         check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
@@ -798,13 +850,14 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
                    "tangent residual");
     }
     const int nl = (int)live.size();
+    const int block = tuned_block(1, nl);
     int done_its = 0;
     while (done_its <= cg_max_its_) {
       run_chunk(2, nl, [&] {
         for (int it = 0; it < chunk; ++it) {
           if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
           timer_begin(t_spmv6_, 0.0);
-          check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 spmv");
+          check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, block, stream_), "cg6 spmv");
           timer_end(t_spmv6_);
           timer_begin(t_upd6_, 0.0);
           check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");

@@ -178,6 +178,8 @@ class Engine {
   void path_free();
   void path_alloc_adj();
   void run_chunk(int kind, int n, const std::function<void()> &body);
+  // Block size of the FP32 SpMV (kind 0) or the 6-RHS SpMV (kind 1) for this RVE size and batch (autotuned).
+  int tuned_block(int kind, int nlist);
   void clear_graphs();
   int bicg_solve(bool transpose, double *x);
   void timer_begin(KernelTimer &t, double bytes);
@@ -218,6 +220,7 @@ class Engine {
 
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  cudaEvent_t tune_ev_[2] = {nullptr, nullptr};
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
   float *d_ke32_ = nullptr, *d_k0g32_ = nullptr, *d_dsh32_ = nullptr;

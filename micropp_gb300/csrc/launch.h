@@ -43,7 +43,9 @@ int mgb_launch_assembly_gather32(const mgb::MeshDev *m, const mgb::Mats *mats, c
                               const float *kesum, const float *dsh32, const mgb::Inst *insts, const int *list,
                               int nlist, cudaStream_t s);
 int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
-int mgb_launch_cg32_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// block: 64, 128 or 256 threads (any other value: 128).
+int mgb_launch_cg32_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int block,
+                         cudaStream_t s);
 int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                             unsigned int *active_count, cudaStream_t s);
@@ -52,7 +54,8 @@ int mgb_launch_axpy_du32(const mgb::MeshDev *m, double *u, const float *du, doub
 int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
                            cudaStream_t s);
-int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int block,
+                        cudaStream_t s);
 int mgb_launch_cg6_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_cg6_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s);

@@ -54,9 +54,9 @@ __device__ __forceinline__ size_t ell32_diag(const MeshDev &m, int n, int d) {
 
 constexpr int kRowsPerThread = 4;   // vector kernels: rows per thread
 constexpr int kSpmvNodes = 4;       // FP32 SpMV: consecutive nodes per thread (one 16-byte load per entry)
-constexpr int kSpmvBlock = 128;
+// Block sizes of the two SpMVs are template parameters (64, 128 or 256 threads), picked per RVE size and batch
+// by the engine's autotuner.
 constexpr int kSpmv6Nodes = 2;      // 6-RHS SpMV: consecutive nodes per thread (one 8-byte load per entry)
-constexpr int kSpmv6Block = 128;
 
 __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
 // (np is a multiple of 32 and the group starts at a multiple of 4), and the 6 neighbours a group row needs
 // along x are loaded once for the 3 x-slots.  A boundary node of the group is an identity row: its stencil
 // sum (taken over clamped neighbour indices) is discarded.
-__global__ void __launch_bounds__(kSpmvBlock) k_cg32_spmv(MeshDev m, const Inst *insts, const int *list) {
+template <int B>
+__global__ void __launch_bounds__(B) k_cg32_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg->done) return;
   const int n0 = (blockIdx.x * blockDim.x + threadIdx.x) * kSpmvNodes;
@@ -414,7 +415,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
 // AP = K P for the six right-hand sides on the full stencil, one pass over K for all six; kSpmv6Nodes
 // consecutive nodes per thread, so each ELL entry of the pair is one 8-byte load and the 4 neighbours a pair
 // row needs along x are loaded once for the 3 x-slots.  The last block sets alpha_i.
-__global__ void __launch_bounds__(kSpmv6Block) k_cg6_spmv(MeshDev m, const Inst *insts, const int *list) {
+template <int B>
+__global__ void __launch_bounds__(B) k_cg6_spmv(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg6->all_done) return;
   const int n0 = (blockIdx.x * blockDim.x + threadIdx.x) * kSpmv6Nodes;
@@ -791,9 +793,16 @@ int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, 
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, int block,
+                         cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_spmv<<<dim3(cdiv(cdiv(m->nn, kSpmvNodes), kSpmvBlock), nlist), kSpmvBlock, 0, s>>>(*m, insts, list);
+  const size_t units = cdiv(m->nn, kSpmvNodes);
+  if (block == 64)
+    k_cg32_spmv<64><<<dim3(cdiv(units, 64), nlist), 64, 0, s>>>(*m, insts, list);
+  else if (block == 256)
+    k_cg32_spmv<256><<<dim3(cdiv(units, 256), nlist), 256, 0, s>>>(*m, insts, list);
+  else
+    k_cg32_spmv<128><<<dim3(cdiv(units, 128), nlist), 128, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
@@ -838,9 +847,15 @@ int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list,
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, int nlist, int block, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_spmv<<<dim3(cdiv(cdiv(m->nn, kSpmv6Nodes), kSpmv6Block), nlist), kSpmv6Block, 0, s>>>(*m, insts, list);
+  const size_t units = cdiv(m->nn, kSpmv6Nodes);
+  if (block == 64)
+    k_cg6_spmv<64><<<dim3(cdiv(units, 64), nlist), 64, 0, s>>>(*m, insts, list);
+  else if (block == 256)
+    k_cg6_spmv<256><<<dim3(cdiv(units, 256), nlist), 256, 0, s>>>(*m, insts, list);
+  else
+    k_cg6_spmv<128><<<dim3(cdiv(units, 128), nlist), 128, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 
