@@ -61,7 +61,8 @@ struct micropp3_config {
   double cg_abs_tol;      /* honoured (reference: CG_ABS_TOL = 1e-50) */
   double cg_rel_tol;      /* honoured (reference: CG_REL_TOL = 1e-5) */
   int calc_ctan_lin;
-  int use_A0;             /* accepted for layout compatibility; the GPU path always assembles K */
+  int use_A0;             /* FP64 form: the first its_with_A0 Newton iterations solve with the Jacobian at
+                           * u = 0 (micropp.cpp:128-143, solve.cpp:55-66); ignored by the mixed form */
   int its_with_A0;
   int lin_stress;
   int write_log;

@@ -148,6 +148,26 @@ Engine::Engine(const micropp3_config &cfg) {
   Vm_ /= mesh_.vol_tot;
   Vf_ /= mesh_.vol_tot;
 
+  // A0 (micropp.cpp:128-143): the Jacobian at u = 0 without history, assembled once before the linear ctan
+  // (whose solves use it).  FP64 form only: the mixed form always assembles its FP32 Jacobian.
+  use_A0_ = cfg.use_A0 != 0 && precision_ == MICROPP3_FP64;
+  its_with_A0_ = cfg.its_with_A0;
+  if (use_A0_) {
+    ensure_slots(1);
+    d_A0_ = dalloc<double>((size_t)kEllPerNode * mesh_.np, "A0");
+    check(cudaMemsetAsync(slots_[0].u, 0, nndim() * sizeof(double), stream_), "A0 u");
+    Inst &I = h_insts_[0];
+    I.vars_old = nullptr;
+    I.has_vars_old = 0;
+    I.vals = d_A0_;
+    upload_insts();
+    upload_list({0});
+    launches_ += 9;
+    check_launch(mgb_launch_assembly(&mesh_, &mats_, d_etype_, d_dsh_, d_ke_, d_insts_, d_list_, 1, stream_), "A0");
+    I.vals = slots_[0].vals;
+    upload_insts();
+  }
+
   std::memset(ctan_lin_, 0, sizeof(ctan_lin_));
   if (calc_ctan_lin_ && n_fe > 0) calc_ctan_lin();
   for (auto &g : gps_) {
@@ -182,6 +202,7 @@ Engine::~Engine() {
   dfree(d_k0g32_);
   dfree(d_dsh32_);
   dfree(d_bnodes_);
+  dfree(d_A0_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
   for (cudaEvent_t e : tune_ev_)
@@ -947,8 +968,15 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     const int na = (int)active.size();
     int bicg_its = 0;
     bool have_residual = false;
+    bool a0_iteration = false;
     if (mixed) {
       assemble32(na);
+    } else if (use_A0_ && !exact_tangent_ && res[idx[0]].its < its_with_A0_) {
+      // solve.cpp:55-66: this iteration solves with A0 (every active slot started this Newton together, so
+      // they share the iteration count)
+      for (int s : active) h_insts_[s].vals = d_A0_;
+      upload_insts();
+      a0_iteration = true;
     } else {
       timer_begin(t_asm_, (double)na * (8.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
       launches_ += 9;
@@ -1032,6 +1060,10 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     } else {
       cg_solve(active);
       check_launch(mgb_launch_add_du(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+      if (a0_iteration) {
+        for (int s : active) h_insts_[s].vals = slots_[s].vals;
+        upload_insts();
+      }
     }
     if (!have_residual) {
       residual(active);

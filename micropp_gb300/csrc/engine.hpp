@@ -203,6 +203,9 @@ class Engine {
   int nsubiterations_ = 10;
   int precision_ = 0, ctan_mode_ = 0;
   bool exact_tangent_ = false;  // FP64 Newton with the exact tangent and BiCGSTAB corrections (paths, slot 0)
+  bool use_A0_ = false;         // micropp.cpp:128-143: the first its_with_A0 FP64 Newton iterations solve with A0
+  int its_with_A0_ = 1;
+  double *d_A0_ = nullptr;      // the FP64 Jacobian at u = 0 without history
   bool last_bicg_converged_ = true;
   std::vector<std::array<double, 6>> predict_de_;  // strain increments of the next newton() call's predictor
 

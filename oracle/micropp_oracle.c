@@ -46,6 +46,15 @@ typedef struct {
   int nr_its, nr_solver_its, nr_converged;
 } orc_gp;
 
+typedef struct {
+  int n[3], nn, nrow;
+  int *cols;
+  double *vals;
+  int max_its;
+  double min_err, rel_err;
+  double *k, *r, *z, *p, *Ap;
+} orc_ell;
+
 struct orc_rve {
   int ngp, nx, ny, nz, nn, nndim, nex, ney, nez, nelem, nvars;
   double lx, ly, lz, dx, dy, dz, wg, vol_tot, ivol, evol;
@@ -60,16 +69,9 @@ struct orc_rve {
   double ctan_lin[NVOI * NVOI];
   double Vm, Vf;
   orc_gp *gp;
+  int use_A0, its_with_A0, nA0;
+  orc_ell *A0; /* micropp.cpp:128-143: the Jacobian at u = 0, one per OpenMP thread (it holds CG work vectors) */
 };
-
-typedef struct {
-  int n[3], nn, nrow;
-  int *cols;
-  double *vals;
-  int max_its;
-  double min_err, rel_err;
-  double *k, *r, *z, *p, *Ap;
-} orc_ell;
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Configuration                                                                                      */
@@ -726,7 +728,8 @@ static int calc_vars_new(const orc_rve *h, const double *u, const double *vold, 
   return nl;
 }
 
-/* newton_raphson (solve.cpp:28-82), without the A0 shortcut (use_A0 is off in the C ABI). */
+/* newton_raphson (solve.cpp:28-82); with use_A0 the first its_with_A0 iterations solve with A0
+ * (solve.cpp:55-66). */
 static void newton_raphson(const orc_rve *h, orc_ell *A, double *b, double *u, double *du, const double strain[6],
                            const double *vars, int *its_out, int *solver_its_out, int *conv_out) {
   int its = 0, solver_its = 0, converged = 0;
@@ -738,9 +741,19 @@ static void newton_raphson(const orc_rve *h, orc_ell *A, double *b, double *u, d
       converged = 1;
       break;
     }
-    assembly_mat(h, A, u, vars);
+    orc_ell *A_ptr;
+    if (!h->use_A0 || its > (h->its_with_A0 - 1)) {
+      assembly_mat(h, A, u, vars);
+      A_ptr = A;
+    } else {
+#ifdef _OPENMP
+      A_ptr = &h->A0[omp_get_thread_num()];
+#else
+      A_ptr = &h->A0[0];
+#endif
+    }
     double cg_err;
-    solver_its += ell_solve_cgpd(A, b, du, &cg_err);
+    solver_its += ell_solve_cgpd(A_ptr, b, du, &cg_err);
     for (int i = 0; i < h->nndim; ++i) u[i] += du[i];
     norm = assembly_rhs(h, u, vars, b);
     its++;
@@ -970,6 +983,25 @@ orc_rve *orc_new(const struct orc_config *c) {
   h->Vm /= h->vol_tot;
   h->Vf /= h->vol_tot;
 
+  /* A0 (micropp.cpp:128-143), before the linear ctan whose solves use it */
+  h->use_A0 = c->use_A0;
+  h->its_with_A0 = c->its_with_A0;
+  if (h->use_A0) {
+#ifdef _OPENMP
+    h->nA0 = omp_get_max_threads();
+#else
+    h->nA0 = 1;
+#endif
+    h->A0 = (orc_ell *)calloc(h->nA0, sizeof(orc_ell));
+    const int ns[3] = {h->nx, h->ny, h->nz};
+    double *u0 = (double *)calloc(h->nndim, sizeof(double));
+    for (int i = 0; i < h->nA0; ++i) {
+      ell_init(&h->A0[i], ns, h->cg_abs_tol, h->cg_rel_tol, h->cg_max_its);
+      assembly_mat(h, &h->A0[i], u0, NULL);
+    }
+    free(u0);
+  }
+
   memset(h->ctan_lin, 0, sizeof(h->ctan_lin));
   if (c->calc_ctan_lin && n_fe > 0) calc_ctan_lin_fe(h);
 
@@ -995,6 +1027,8 @@ void orc_free(orc_rve *h) {
   }
   free(h->gp);
   free(h->elem_type);
+  for (int i = 0; i < h->nA0; ++i) ell_free(&h->A0[i]);
+  free(h->A0);
   free(h);
 }
 

@@ -139,6 +139,23 @@ def test_subiterations_mixture_rule_one_way(gpu_lib, seed):
     _compare_steps(g, o, steps)
 
 
+@pytest.mark.parametrize("law,its_with_A0", [(0, 1), (1, 2)])
+def test_use_A0(gpu_lib, law, its_with_A0):
+    """use_A0: the first its_with_A0 Newton iterations (also of the linear-ctan and the perturbed solves) solve
+    with the Jacobian at u = 0 (micropp.cpp:128-143, solve.cpp:55-66); same costs as the oracle, which is
+    pinned to the compiled reference on this option."""
+    import micropp_gb300 as mg
+    lawp = [(2, 1e7, 0.25, 0, 0, 1e5), (1, 1e7, 0.3, 1e5, 1e4, 0)][law]
+    mats = (lawp, (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0))
+    kw = dict(ngp=2, micro_type=1, geo=(0.25, 0, 0, 0), mats=mats, coupling=[2, 1], lin_stress=0, nr_max_its=8,
+              use_A0=1, its_with_A0=its_with_A0)
+    o = orc.OracleRVE(oracle_config(5, **kw))
+    g = mg.Micropp(gpu_config(5, **kw))
+    assert rel_err(g.ctan_lin(), o.ctan_lin()) < TOL_CTAN_LIN
+    rng = np.random.default_rng(law)
+    _compare_steps(g, o, [[rng.uniform(-2e-2, 2e-2, 6) for _ in range(2)] for _ in range(3)])
+
+
 def test_restart_roundtrip(gpu_lib, tmp_path, monkeypatch):
     """write_restart produces the reference's bytes; read_restart into a new handle continues identically."""
     import micropp_gb300 as mg

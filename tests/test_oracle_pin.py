@@ -107,6 +107,35 @@ def test_live_random_paths(seed):
 
 
 @needs_ref
+@pytest.mark.parametrize("law,its_with_A0", [(0, 1), (1, 2)])
+def test_live_use_A0(law, its_with_A0):
+    """use_A0 (micropp.cpp:128-143, solve.cpp:55-66): the first its_with_A0 Newton iterations solve with the
+    Jacobian at u = 0, also in the constructor's linear solves and the perturbed ctan solves."""
+    lawp = [(2, 1e7, 0.25, 0, 0, 1e5), (1, 1e7, 0.3, 1e5, 1e4, 0)][law]
+    mats = [orc.material(*lawp), orc.material(0, 1e8, 0.25), orc.material(0, 1e7, 0.25)]
+    cfg = orc.make_config(5, ngp=2, micro_type=1, geo=(0.25, 0, 0, 0), mats=mats, coupling=[2, 1], lin_stress=0,
+                          nr_max_its=8, use_A0=1, its_with_A0=its_with_A0)
+    a, b = orc.OracleRVE(cfg), orc.RefRVE(cfg)
+    assert np.array_equal(a.ctan_lin(), b.ctan_lin())
+    rng = np.random.default_rng(law)
+    for step in range(3):
+        for gp in range(2):
+            e = rng.uniform(-2e-2, 2e-2, 6)
+            a.set_strain(gp, e)
+            b.set_strain(gp, e)
+        a.homogenize()
+        b.homogenize()
+        for gp in range(2):
+            assert np.array_equal(a.get_stress(gp), b.get_stress(gp))
+            assert np.array_equal(a.get_ctan(gp), b.get_ctan(gp))
+            assert a.get_cost(gp) == b.get_cost(gp)
+            assert a.has_converged(gp) == b.has_converged(gp)
+            assert np.array_equal(a.u(gp, 1), b.u(gp, 1))
+        a.update_vars()
+        b.update_vars()
+
+
+@needs_ref
 def test_live_restart_format(tmp_path, monkeypatch):
     """Restart files: byte-identical to the reference's micropp-restart-<rank>-<id>.bin."""
     monkeypatch.chdir(tmp_path)
