@@ -360,7 +360,7 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     newton = [h.newton(gp) for h, gp in points]  # (Newton its, CG its, converged) of the last solve
     finite = bool(np.isfinite(out_s).all() and np.isfinite(out_c).all())
     stats = {}
-    for fam in ("spmv", "spmv6", "cg_update", "cg6_update", "assembly", "residual"):
+    for fam in ("spmv", "spmv6", "cg_update", "cg6_update", "mg", "mg6", "mg_coarse", "assembly", "residual"):
         tot = [h.kernel_stats(fam) for h in handles]
         stats[fam] = (sum(t[0] for t in tot), sum(t[1] for t in tot), sum(t[2] for t in tot))
     for h in handles:
@@ -378,13 +378,19 @@ def roofline_of(res, n, peak, peak_kind):
     """Roofline record of the form's dominant linear-algebra kernel (most device time)."""
     nrow = 3 * (n + 1) ** 3
     fp32 = FORMS[res["form"]]["cfg"]["precision"] == 1
-    cands = {"spmv": res["stats"]["spmv"], "spmv6": res["stats"]["spmv6"]}
+    cands = {k: res["stats"][k] for k in ("spmv", "spmv6", "mg", "mg6")}
     fam = max(cands, key=lambda k: cands[k][1])
     nk, ms, by = cands[fam]
     achieved = by / (ms / 1e3) / 1e9 if ms > 0 else None
-    # algorithmic bytes of one RVE's SpMV: 81 values per row, x read once, y written once (per right-hand side)
+    # algorithmic bytes of one RVE's SpMV: 81 values per row, x read once, y written once (per right-hand side);
+    # the multigrid level-0 passes also read b
     if fam == "spmv6":
         name, per = "k_cg6_spmv (FP32 ELL SpMV, 6 right-hand sides)", nrow * (81 * 4 + 12 * 4)
+    elif fam == "mg6":
+        name, per = "k_mg_resid / k_mg_post0 (FP32 ELL SpMV of the V-cycle's fine level, 6 right-hand sides)", \
+            nrow * (81 * 4 + 18 * 4)
+    elif fam == "mg":
+        name, per = "k_mg_resid / k_mg_post0 (FP32 ELL SpMV of the V-cycle's fine level)", nrow * (81 * 4 + 3 * 4)
     elif fp32:
         name, per = "k_cg32_spmv (FP32 ELL SpMV + p.Ap)", nrow * (81 * 4 + 2 * 4)
     else:

@@ -34,6 +34,16 @@ enum {
   MICROPP3_CTAN_IMPLICIT = 1  /* implicit differentiation at the converged state: one 6-RHS tangent solve */
 };
 
+/* Preconditioner of the FP32 CG solves (the mixed form's Newton corrections and the implicit ctan's 6-RHS
+ * tangent solve). */
+enum {
+  MICROPP3_PRECOND_AUTO = 0,   /* multigrid where the grid coarsens (at least 4 elements along every axis and
+                                * more than 4 along one), Jacobi otherwise */
+  MICROPP3_PRECOND_JACOBI = 1, /* point Jacobi, as the reference's DPCG */
+  MICROPP3_PRECOND_MG = 2      /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
+                                * damped-Jacobi smoothing; every axis coarsens to ceil(elements / 2) */
+};
+
 /* Per-RVE status word of the last homogenize(). */
 enum {
   MICROPP3_STATUS_OK = 0,
@@ -69,7 +79,9 @@ struct micropp3_config {
   const int *elem_type;   /* optional element phase map, nelem entries in glo_elem order (0, 1 or 2) */
   int precision;          /* MICROPP3_FP64 | MICROPP3_MIXED */
   int ctan_mode;          /* MICROPP3_CTAN_PERTURB | MICROPP3_CTAN_IMPLICIT */
-  int reserved[4];        /* zero */
+  int precond;            /* MICROPP3_PRECOND_*: preconditioner of the FP32 solves (mixed-form Newton, implicit
+                           * ctan); the FP64 Newton always uses the reference's Jacobi CG */
+  int reserved[3];        /* zero */
 };
 
 /* The reference defaults (types.hpp:43-63 with params.hpp:32-35 and ell.hpp:33-35), FP64, perturbation
@@ -105,13 +117,18 @@ void micropp3_get_u(const struct micropp3 *self, int gp_id, int which, double *o
 void micropp3_get_elem_type(const struct micropp3 *self, int *out);
 void micropp3_get_ctan_lin(const struct micropp3 *self, double *out36);
 
+/* Levels of the multigrid preconditioner in use (0: Jacobi). */
+int micropp3_get_mg_levels(const struct micropp3 *self);
+
 /* Device time of the last homogenize() (CUDA events on the handle's stream), in milliseconds. */
 double micropp3_last_homogenize_ms(const struct micropp3 *self);
 
 /* Kernel timing.  When enabled, every launch of the named kernel family is bracketed by CUDA events on the
  * launching stream; micropp3_kernel_stats returns the launch count, the summed device time (ms) and the
  * algorithmic bytes moved by those launches.  Families: "spmv" (the Newton CG's SpMV), "cg_update" (its two
- * vector kernels), "spmv6" and "cg6_update" (the same for the 6-RHS tangent CG), "assembly", "residual". */
+ * vector kernels), "spmv6" and "cg6_update" (the same for the 6-RHS tangent CG), "mg" and "mg6" (the two
+ * fine-level operator passes of the multigrid V-cycles of the two CGs), "mg_coarse" (the rest of the V-cycles),
+ * "assembly" (with the multigrid Galerkin operators), "residual". */
 void micropp3_set_kernel_timing(struct micropp3 *self, int enable);
 /* CUDA graphs: the CG iterations run in chunks captured once per (solver, batch size) and replayed
  * (default on; chunks are launched directly while kernel timing is on). */

@@ -23,6 +23,7 @@ MATERIAL_ELASTIC, MATERIAL_PLASTIC, MATERIAL_DAMAGE = 0, 1, 2
  MIC3D_FIBS_20_DISORDER) = range(13)
 FP64, MIXED = 0, 1
 CTAN_PERTURB, CTAN_IMPLICIT = 0, 1
+PRECOND_AUTO, PRECOND_JACOBI, PRECOND_MG = 0, 1, 2
 STATUS_OK, STATUS_NEWTON_MAX_ITS, STATUS_CG_MAX_ITS, STATUS_NONFINITE = 0, 1, 2, 4
 
 
@@ -45,7 +46,7 @@ class Config(C.Structure):
                 ("cg_rel_tol", C.c_double), ("calc_ctan_lin", C.c_int), ("use_A0", C.c_int),
                 ("its_with_A0", C.c_int), ("lin_stress", C.c_int), ("write_log", C.c_int),
                 ("elem_type", C.POINTER(C.c_int)), ("precision", C.c_int), ("ctan_mode", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("precond", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class Handle(C.Structure):
@@ -108,6 +109,7 @@ def load():
         "micropp3_set_kernel_timing": (None, [H, C.c_int]),
         "micropp3_kernel_stats": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_long), dp, dp]),
         "micropp3_total_cg_its": (C.c_long, [H]),
+        "micropp3_get_mg_levels": (C.c_int, [H]),
         "micropp3_kernel_launches": (C.c_long, [H]),
         "micropp3_path_forward": (C.c_int, [H, C.c_int, dp, dp, C.c_int, dp]),
         "micropp3_path_vjp": (C.c_int, [H, dp, dp, dp]),
@@ -307,6 +309,9 @@ class Micropp:
 
     def total_cg_its(self):
         return self._call("micropp3_total_cg_its")
+
+    def mg_levels(self):
+        return self._call("micropp3_get_mg_levels")
 
     def kernel_launches(self):
         return self._call("micropp3_kernel_launches")

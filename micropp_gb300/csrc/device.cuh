@@ -86,6 +86,22 @@ struct InstOut {
   int pad;
 };
 
+// Geometric multigrid hierarchy of one instance (mixed form).  Level 0 is the fine grid (the instance's vals32,
+// kinv32 and CG vectors); level l >= 1 coarsens every axis of level l-1 to ceil(elements / 2).  A level's
+// operator is the Galerkin product P^T A P in the fine grid's stencil ELL layout; its vectors hold up to 6
+// right-hand sides component-major, v[(r * 3 + d) * np_l + n], and are zero on boundary nodes.
+constexpr int kMgMaxLevels = 8;
+
+struct MgLevel {
+  float *vals;             // 243 * np_l (level >= 1)
+  float *kinv;             // 3 * nn_l, node-interleaved; 1 on boundary rows
+  float *b, *x, *y, *t;    // right-hand side, iterate, Jacobi ping-pong partner, residual / prolonged iterate
+};
+
+struct MgInst {
+  MgLevel lv[kMgMaxLevels];
+};
+
 struct Inst {
   double *u, *du, *b, *r, *z, *p, *Ap, *kinv, *vals, *be;
   const double *vars_old;  // NULL: every law reads zeros (the reference's nullptr history)
@@ -103,6 +119,7 @@ struct Inst {
   double *X6, *F6;
   float *R6, *Z6, *P6, *AP6, *D6;
   Cg6State *cg6;
+  MgInst *mg;              // multigrid hierarchy (NULL: Jacobi-preconditioned CG)
   double strain[6];
   int has_vars_old;        // J2 evolute writes only when a history buffer exists (material.cpp:168-181)
   int pad;

@@ -39,6 +39,12 @@ constexpr int kTangentSweeps = 4;
 // Lowest relative tolerance asked of the mixed form's FP32 Newton CG.
 constexpr double kFp32CgFloor = 1.0e-6;
 
+// Multigrid preconditioner of the FP32 solves: damped-Jacobi weight of the smoothers, pairs of Jacobi sweeps
+// on the coarsest level after the first one (9 sweeps), CG iterations between polls of the active count.
+constexpr float kMgOmega = 0.6f;
+constexpr int kMgCoarsePairs = 4;
+constexpr int kMgChunk = 4;
+
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
 }  // namespace
@@ -85,6 +91,41 @@ Engine::Engine(const micropp3_config &cfg) {
   // colouring assembly.
   gather32_ = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
   for (int e = 0; e < mesh_.nelem && gather32_; ++e) gather32_ = mats_.m[etype_[e]].type != 1;
+  // Multigrid levels: every axis of n elements coarsens to ceil(n / 2) while each axis keeps at least 4
+  // elements and some axis has more than 4.
+  {
+    const int pc = cfg.precond;
+    if (pc != MICROPP3_PRECOND_AUTO && pc != MICROPP3_PRECOND_JACOBI && pc != MICROPP3_PRECOND_MG)
+      throw std::invalid_argument("precond must be MICROPP3_PRECOND_AUTO, _JACOBI or _MG");
+    const bool fp32_solves = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
+    if (pc == MICROPP3_PRECOND_MG && !fp32_solves)
+      throw std::invalid_argument("the multigrid preconditioner applies to the FP32 solves (MICROPP3_MIXED or "
+                                  "MICROPP3_CTAN_IMPLICIT); the FP64 Newton keeps the reference's Jacobi CG");
+    mg_mesh_.assign(1, mesh_);
+    int ne[3] = {mesh_.nex, mesh_.ney, mesh_.nez};
+    while ((int)mg_mesh_.size() < kMgMaxLevels) {
+      const int lo = std::min(ne[0], std::min(ne[1], ne[2])), hi = std::max(ne[0], std::max(ne[1], ne[2]));
+      if (lo < 4 || hi <= 4) break;
+      for (int &e : ne) e = (e + 1) / 2;
+      MeshDev c{};
+      c.nex = ne[0];
+      c.ney = ne[1];
+      c.nez = ne[2];
+      c.nelem = ne[0] * ne[1] * ne[2];
+      c.nx = ne[0] + 1;
+      c.ny = ne[1] + 1;
+      c.nz = ne[2] + 1;
+      c.nxny = c.nx * c.ny;
+      c.nn = c.nxny * c.nz;
+      c.np = (c.nn + 31) / 32 * 32;
+      mg_mesh_.push_back(c);
+    }
+    mg_ = fp32_solves && pc != MICROPP3_PRECOND_JACOBI && mg_mesh_.size() >= 2;
+    if (pc == MICROPP3_PRECOND_MG && !mg_)
+      throw std::invalid_argument("the multigrid preconditioner needs at least 4 elements along every axis and "
+                                  "more than 4 along one");
+    if (!mg_) mg_mesh_.clear();
+  }
 
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   check(cudaEventCreate(&ev0_), "event");
@@ -190,7 +231,7 @@ Engine::~Engine() {
   clear_graphs();
   path_free();
   free_slots();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_})
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_})
     for (auto &e : t->pool) {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
@@ -401,6 +442,10 @@ double Engine::slot_bytes() const {
     b += 4.0 * (kEllPerNode * np + nd + (gather32_ ? 64.0 * mesh_.nelem : 0.0));
   if (precision_ == MICROPP3_MIXED) b += 4.0 * 5.0 * nd;
   if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += (8.0 * 2.0 + 4.0 * 5.0) * 18.0 * np;
+  if (mg_) {
+    b += 4.0 * 18.0 * np;
+    for (size_t l = 1; l < mg_mesh_.size(); ++l) b += 4.0 * (kEllPerNode + 3.0 + 4.0 * 18.0) * mg_mesh_[l].np;
+  }
   return b;
 }
 
@@ -456,6 +501,28 @@ void Engine::ensure_slots(int n) {
       w.D6 = dalloc<float>(n6, "D6");
       w.cg6 = dalloc<Cg6State>(1, "cg6 state");
     }
+    if (mg_) {
+      // level 0: the residual / prolonged iterate (6 right-hand sides component-major, or 1 node-interleaved);
+      // levels >= 1: the Galerkin operator, its inverse diagonal and four vectors of 6 right-hand sides
+      MgInst h{};
+      auto buf = [&](size_t n, const char *what) {
+        float *p = dalloc<float>(n, what);
+        w.mg_bufs.push_back(p);
+        return p;
+      };
+      h.lv[0].t = buf((size_t)18 * mesh_.np, "multigrid level-0 residual");
+      for (size_t l = 1; l < mg_mesh_.size(); ++l) {
+        const size_t np = mg_mesh_[l].np;
+        h.lv[l].vals = buf((size_t)kEllPerNode * np, "multigrid operator");
+        h.lv[l].kinv = buf((size_t)3 * np, "multigrid diagonal");
+        h.lv[l].b = buf((size_t)18 * np, "multigrid vector");
+        h.lv[l].x = buf((size_t)18 * np, "multigrid vector");
+        h.lv[l].y = buf((size_t)18 * np, "multigrid vector");
+        h.lv[l].t = buf((size_t)18 * np, "multigrid vector");
+      }
+      w.mg = dalloc<MgInst>(1, "multigrid hierarchy");
+      check(cudaMemcpy(w.mg, &h, sizeof(MgInst), cudaMemcpyHostToDevice), "multigrid hierarchy upload");
+    }
     check(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), stream_), "ticket");
     check(cudaMemsetAsync(w.out, 0, sizeof(InstOut), stream_), "out");
   }
@@ -474,6 +541,7 @@ void Engine::ensure_slots(int n) {
     I.du32 = w.du32;
     I.X6 = w.X6; I.F6 = w.F6; I.R6 = w.R6; I.Z6 = w.Z6; I.P6 = w.P6; I.AP6 = w.AP6; I.D6 = w.D6; I.cg6 = w.cg6;
     I.gpd = w.gpd;
+    I.mg = w.mg;
     I.vars_old = nullptr;
     I.vars_new = w.vars_aux;
   }
@@ -490,6 +558,9 @@ void Engine::free_slots() {
       dfree(p);
     for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6, w.gpd})
       dfree(p);
+    for (float *p : w.mg_bufs) dfree(p);
+    w.mg_bufs.clear();
+    dfree(w.mg);
     dfree(w.ticket);
     dfree(w.cg);
     dfree(w.cg6);
@@ -537,7 +608,7 @@ void Engine::sync() { check(cudaStreamSynchronize(stream_), "stream synchronize"
 // off.  The kernels read the instance list and the CG states from device memory, so one capture serves every
 // later solve with the same number of listed instances.
 void Engine::run_chunk(int kind, int n, const std::function<void()> &body) {
-  const bool timing = t_spmv_.enabled || t_update_.enabled || t_spmv6_.enabled || t_upd6_.enabled;
+  const bool timing = t_spmv_.enabled || t_update_.enabled || t_spmv6_.enabled || t_upd6_.enabled || t_mg1_.enabled;
   if (!graphs_ || timing) {
     body();
     return;
@@ -653,7 +724,7 @@ void Engine::timer_end(KernelTimer &t) {
 
 void Engine::set_kernel_timing(bool on) {
   sync();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_}) {
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_}) {
     t->enabled = on;
     t->used = 0;
     t->launches = 0;
@@ -669,6 +740,9 @@ bool Engine::kernel_stats(const std::string &family, long *launches, double *ms,
   else if (family == "residual") t = &t_res_;
   else if (family == "spmv6") t = &t_spmv6_;
   else if (family == "cg6_update") t = &t_upd6_;
+  else if (family == "mg") t = &t_mg1_;
+  else if (family == "mg6") t = &t_mg6_;
+  else if (family == "mg_coarse") t = &t_mgc_;
   if (!t) return false;
   sync();
   for (size_t i = 0; i < t->used; ++i) {
@@ -759,12 +833,15 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
     check(cudaMemcpyAsync(slots_[slots[a]].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
   }
   launches_ += 1;
-  check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, stream_), "cg32 setup");
+  check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, mg_ ? kMgOmega : 1.0f, stream_), "cg32 setup");
+  if (mg_) {
+    mg_vcycle(1, n, true);
+  }
   const int block = tuned_block(0, n);
   const double nrow = (double)nndim();
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 4);  // per iteration and instance, as in cg_solve
   const double upd_bytes = nrow * 11.0 * 4;
-  const int chunk = (mesh_.nn > 200000) ? 8 : 32;
+  const int chunk = mg_ ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
     run_chunk(1, n, [&] {
@@ -774,7 +851,13 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
         check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, block, stream_), "cg32 spmv");
         timer_end(t_spmv_);
         timer_begin(t_update_, 0.0);
-        check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, stream_), "cg32 update");
+        check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, mg_ ? 1 : 0, kMgOmega, stream_),
+                     "cg32 update");
+        timer_end(t_update_);
+        if (mg_) {
+          mg_vcycle(1, n, false);
+        }
+        timer_begin(t_update_, 0.0);
         check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
         timer_end(t_update_);
       }
@@ -789,6 +872,10 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
     const double its = listed_cg_its(slots);
     timer_add_bytes(t_spmv_, its * spmv_bytes);
     timer_add_bytes(t_update_, its * upd_bytes);
+    if (mg_) {
+      timer_add_bytes(t_mg1_, (its + n) * mg_fine_bytes(1));
+      timer_add_bytes(t_mgc_, (its + n) * mg_coarse_bytes(1));
+    }
   }
 }
 
@@ -808,6 +895,81 @@ void Engine::assemble32(int nlist) {
                  "assembly (FP32)");
   }
   timer_end(t_asm_);
+  if (mg_) mg_rap(nlist);
+}
+
+// Galerkin operators P^T A P of every coarse level, finest first.  Algorithmic bytes: each level's operator
+// read once and the next one written once.
+void Engine::mg_rap(int nlist) {
+  double bytes = 0.0;
+  for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l)
+    bytes += 4.0 * kEllPerNode * (double)(mg_mesh_[l].np + mg_mesh_[l + 1].np);
+  timer_begin(t_asm_, nlist * bytes);
+  for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l) {
+    launches_ += 1;
+    check_launch(mgb_launch_mg_rap(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, (int)l, stream_),
+                 "multigrid Galerkin operator");
+  }
+  timer_end(t_asm_);
+}
+
+// Algorithmic bytes of one V-cycle per instance.  Level 0: the residual and the post-smoother, each 81 values
+// per row, and per right-hand side x (or t) read, b read, the result written.  The rest: on each coarse level
+// above the coarsest two operator passes and about eight vector passes; on the coarsest level the Jacobi
+// sweeps (one operator pass and three vector passes each); the level-0 restriction and prolongation (three
+// vector passes).
+double Engine::mg_fine_bytes(int nr) const {
+  return 2.0 * (double)nndim() * (81.0 * 4 + 3.0 * nr * 4);
+}
+
+double Engine::mg_coarse_bytes(int nr) const {
+  const size_t L = mg_mesh_.size();
+  double b = 3.0 * 4.0 * nr * (double)nndim();
+  for (size_t l = 1; l < L; ++l) {
+    const double nn = mg_mesh_[l].nn, vec = 4.0 * 3.0 * nr * nn, op = 4.0 * kEllPerNode * nn;
+    if (l + 1 < L)
+      b += 2.0 * op + 8.0 * vec;
+    else
+      b += (2.0 * kMgCoarsePairs) * (op + 3.0 * vec);
+  }
+  return b;
+}
+
+// One V-cycle of the nr-RHS CG of the listed instances (their level-0 iterate x0 = w D^-1 r is already
+// written), ending with the level-0 post-smoother that forms z and the CG scalars.
+void Engine::mg_vcycle(int nr, int nlist, bool setup) {
+  const int L = (int)mg_mesh_.size();
+  KernelTimer &fine = (nr == 1) ? t_mg1_ : t_mg6_;
+  for (int l = 0; l + 1 < L; ++l) {
+    if (l == 0) timer_begin(fine, 0.0);
+    check_launch(mgb_launch_mg_resid(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, stream_), "multigrid residual");
+    if (l == 0) {
+      timer_end(fine);
+      timer_begin(t_mgc_, 0.0);
+    }
+    check_launch(mgb_launch_mg_restrict(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, kMgOmega,
+                                        stream_),
+                 "multigrid restriction");
+  }
+  for (int k = 0; k < kMgCoarsePairs; ++k) {
+    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 0, 1, kMgOmega, stream_),
+                 "multigrid coarse sweep");
+    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 1, 0, kMgOmega, stream_),
+                 "multigrid coarse sweep");
+  }
+  for (int l = L - 2; l >= 0; --l) {
+    check_launch(mgb_launch_mg_prolong(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, stream_),
+                 "multigrid prolongation");
+    if (l > 0)
+      check_launch(mgb_launch_mg_jacobi(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, 2, 0, kMgOmega, stream_),
+                   "multigrid post-smoother");
+  }
+  timer_end(t_mgc_);
+  timer_begin(fine, 0.0);
+  check_launch(mgb_launch_mg_post0(&mesh_, d_insts_, d_list_, nlist, nr, kMgOmega, setup ? 1 : 0, stream_),
+               "multigrid level-0 post-smoother");
+  timer_end(fine);
+  launches_ += 2 * (L - 1) + 2 * kMgCoarsePairs + (L - 1) + (L - 2) + 1;
 }
 
 // Implicit ctan of the listed slots at their current u with their vars_old: assemble the FP32 tangent, form
@@ -826,7 +988,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   // write D, R, Z; p-update: read Z, P, write P (per right-hand side).  Credited per instance iteration.
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 6 * 4);
   const double upd6_bytes = nrow * 6.0 * 10.0 * 4;
-  const int chunk = (mesh_.nn > 200000) ? 8 : 32;
+  const int chunk = mg_ ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
   std::vector<int> live = slots;
   std::vector<int> live_idx(n);
   for (int i = 0; i < n; ++i) live_idx[i] = i;
@@ -840,7 +1002,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
     }
     if (sweep > 0) upload_list(live);
     launches_ += 1;
-    check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0, stream_),
+    check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
+                                        mg_ ? kMgOmega : 1.0f, stream_),
                  "tangent residual");
     download_out();
     std::vector<int> next, next_idx;
@@ -867,10 +1030,14 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
         check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
       }
       launches_ += 1;
-      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0, stream_),
+      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
+                                          mg_ ? kMgOmega : 1.0f, stream_),
                    "tangent residual");
     }
     const int nl = (int)live.size();
+    if (mg_) {
+      mg_vcycle(6, nl, true);
+    }
     const int block = tuned_block(1, nl);
     int done_its = 0;
     while (done_its <= cg_max_its_) {
@@ -881,7 +1048,13 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
           check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, block, stream_), "cg6 spmv");
           timer_end(t_spmv6_);
           timer_begin(t_upd6_, 0.0);
-          check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, stream_), "cg6 update");
+          check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, mg_ ? 1 : 0, kMgOmega, stream_),
+                       "cg6 update");
+          timer_end(t_upd6_);
+          if (mg_) {
+            mg_vcycle(6, nl, false);
+          }
+          timer_begin(t_upd6_, 0.0);
           check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
           timer_end(t_upd6_);
         }
@@ -900,6 +1073,10 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
       total_cg_its_ += h_out_[live[a]].cg6_its;
       timer_add_bytes(t_spmv6_, h_out_[live[a]].cg6_its * spmv_bytes);
       timer_add_bytes(t_upd6_, h_out_[live[a]].cg6_its * upd6_bytes);
+      if (mg_) {
+        timer_add_bytes(t_mg6_, (h_out_[live[a]].cg6_its + 1) * mg_fine_bytes(6));
+        timer_add_bytes(t_mgc_, (h_out_[live[a]].cg6_its + 1) * mg_coarse_bytes(6));
+      }
     }
   }
   upload_list(slots);

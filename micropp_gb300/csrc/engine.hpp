@@ -46,6 +46,8 @@ struct Slot {
   double *X6 = nullptr, *F6 = nullptr;
   float *R6 = nullptr, *Z6 = nullptr, *P6 = nullptr, *AP6 = nullptr, *D6 = nullptr;
   float *gpd = nullptr;
+  MgInst *mg = nullptr;          // device copy of the multigrid hierarchy's pointers
+  std::vector<float *> mg_bufs;  // its buffers
   unsigned int *ticket = nullptr;
   CgState *cg = nullptr;
   Cg6State *cg6 = nullptr;
@@ -136,6 +138,8 @@ class Engine {
   // Newton record of step `step` of the last path's forward pass.
   void path_newton(int step, int *its, int *cg_its, int *converged, double *rel_norm) const;
 
+  // Levels of the multigrid preconditioner of the FP32 solves (0: Jacobi).
+  int mg_levels() const { return mg_ ? (int)mg_mesh_.size() : 0; }
   double last_homogenize_ms() const { return last_ms_; }
   void set_graphs(bool on);
   bool graphs() const { return graphs_; }
@@ -182,6 +186,13 @@ class Engine {
   int tuned_block(int kind, int nlist);
   void clear_graphs();
   int bicg_solve(bool transpose, double *x);
+  // Multigrid (engine.cpp): Galerkin operators of the listed slots after an FP32 assembly; one V-cycle of the
+  // 1- or 6-RHS CG of the listed slots, ending with the level-0 post-smoother (setup: start of a solve).
+  void mg_rap(int nlist);
+  void mg_vcycle(int nr, int nlist, bool setup);
+  // Algorithmic bytes of one V-cycle per instance: its two level-0 operator passes, and the rest.
+  double mg_fine_bytes(int nr) const;
+  double mg_coarse_bytes(int nr) const;
   void timer_begin(KernelTimer &t, double bytes);
   void timer_end(KernelTimer &t);
   // Adds algorithmic bytes to a timer whose launches were recorded with 0 bytes.
@@ -202,6 +213,8 @@ class Engine {
   bool lin_stress_ = true, subiterations_ = false, calc_ctan_lin_ = true;
   int nsubiterations_ = 10;
   int precision_ = 0, ctan_mode_ = 0;
+  bool mg_ = false;                 // the FP32 solves are multigrid-preconditioned
+  std::vector<MeshDev> mg_mesh_;    // grids of the multigrid levels (level 0 = mesh_)
   bool exact_tangent_ = false;  // FP64 Newton with the exact tangent and BiCGSTAB corrections (paths, slot 0)
   bool use_A0_ = false;         // micropp.cpp:128-143: the first its_with_A0 FP64 Newton iterations solve with A0
   int its_with_A0_ = 1;
@@ -240,6 +253,7 @@ class Engine {
   long total_cg_its_ = 0;
   long launches_ = 0;  // kernels of this library launched by the handle
   KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_, t_upd6_;
+  KernelTimer t_mg1_, t_mg6_, t_mgc_;  // V-cycles: level-0 passes (1 and 6 RHS), coarse levels and transfers
   PathState path_;
   bool graphs_ = true;                         // CG chunks replayed from captured CUDA graphs
   std::map<long, cudaGraphExec_t> graph_cache_;  // (solver, listed instances) -> executable graph

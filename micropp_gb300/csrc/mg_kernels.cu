@@ -1,0 +1,475 @@
+// mg_kernels.cu -- geometric multigrid preconditioner of the mixed form's FP32 CG solves (1 or 6 right-hand
+// sides).
+//
+// The RVE grid is structured, so a coarse level is again a structured grid: every axis of n elements becomes
+// ceil(n / 2) elements, coarse node I sits on fine node 2I (the last coarse interval is one fine element wide
+// when n is odd), and the prolongation P is trilinear: a fine node with even index along an axis takes its
+// coarse parent with weight 1, an odd one its two neighbours with weight 1/2.  Corrections vanish on boundary
+// nodes (Dirichlet rows), so P only couples interior nodes.  The coarse operator is the Galerkin product
+// A_c = P^T A P; with trilinear P and a 27-point operator it is again a 27-point operator of 3x3 blocks, so
+// every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].
+//
+// The preconditioner is one V-cycle with damped Jacobi (weight kMgOmega) as pre- and post-smoother and a
+// fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric operation, so the
+// V-cycle is a fixed symmetric preconditioner and the CG recurrences stay those of preconditioned CG.
+//
+//   level 0:   x0 = w D^-1 r                    (written by the CG update kernel)
+//   l < L-1:   t_l = b_l - A_l x_l;  b_{l+1} = P^T t_l;  x_{l+1} = w D^-1 b_{l+1}
+//   coarsest:  (sweeps - 1) x Jacobi sweeps, ping-pong between x and y
+//   l >= 1:    t_l = x_l + P x_{l+1};  x_l = t_l + w D^-1 (b_l - A_l t_l)
+//   level 0:   t_0 = x_0 + P x_1;  z = t_0 + w D^-1 (r - A t_0), with r.z and the CG scalars
+//
+// Level 0 vectors are the CG's own: node-interleaved r32/z32 for one right-hand side, component-major R6/Z6
+// for six; the level-0 residual and prolongation go to lv[0].t (3 * nn or 18 * np floats).  Every kernel
+// writes zeros on boundary nodes, so coarse vectors never carry values there.  Launch order on one stream is
+// the only synchronisation; reductions use the last-block ticket of reduce.cuh.
+#include "device.cuh"
+#include "launch.h"
+#include "reduce.cuh"
+
+namespace mgb {
+namespace {
+
+constexpr int kMgBlock = 128;
+
+// Index of component (r, d) of node n in a level's vector: node-interleaved for a single right-hand side on
+// level 0 (RM), component-major otherwise.
+template <bool RM>
+__device__ __forceinline__ size_t vix(int r, int d, int n, size_t np) {
+  return RM ? (size_t)n * 3 + d : (size_t)(r * 3 + d) * np + n;
+}
+
+__device__ __forceinline__ bool on_boundary(const MeshDev &m, int n, int &i, int &j, int &k) {
+  i = n % m.nx;
+  j = (n / m.nx) % m.ny;
+  k = n / m.nxny;
+  return i == 0 || j == 0 || k == 0 || i == m.nx - 1 || j == m.ny - 1 || k == m.nz - 1;
+}
+
+__device__ __forceinline__ float half_pow(int a) { return a == 0 ? 1.0f : (a == 1 || a == -1) ? 0.5f : 0.0f; }
+
+template <int NR>
+__device__ __forceinline__ bool inst_done(const Inst &I) {
+  return NR == 1 ? I.cg->done != 0 : I.cg6->all_done != 0;
+}
+
+// Buffers of level l of an instance (level 0: the CG's vectors and the fine operator).
+struct LvView {
+  const float *vals, *kinv;
+  float *b, *x, *y, *t;
+};
+
+template <int NR>
+__device__ __forceinline__ LvView view(const Inst &I, int l) {
+  const MgLevel &L = I.mg->lv[l];
+  LvView v;
+  if (l == 0) {
+    v.vals = I.vals32;
+    v.kinv = I.kinv32;
+    v.b = NR == 1 ? I.r32 : I.R6;
+    v.x = NR == 1 ? I.z32 : I.Z6;
+    v.y = nullptr;
+  } else {
+    v.vals = L.vals;
+    v.kinv = L.kinv;
+    v.b = L.b;
+    v.x = L.x;
+    v.y = L.y;
+  }
+  v.t = L.t;
+  return v;
+}
+
+// which: 0 = x, 1 = y, 2 = t
+__device__ __forceinline__ float *pick(const LvView &v, int which) { return which == 0 ? v.x : which == 1 ? v.y : v.t; }
+
+// y = A x at interior node n for NR right-hand sides (slot order, then column order, as the CG SpMVs).
+template <int NR, bool RM, bool STREAM>
+__device__ __forceinline__ void apply_node(const MeshDev &m, const float *__restrict__ vals,
+                                           const float *__restrict__ x, int n, float (&y)[NR * 3]) {
+  const size_t np = m.np;
+#pragma unroll
+  for (int c = 0; c < NR * 3; ++c) y[c] = 0.f;
+#pragma unroll 3
+  for (int s = 0; s < 27; ++s) {
+    const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
+    float K[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const float *a = vals + (size_t)(s * 9 + q) * np + n;
+      K[q] = STREAM ? __ldcs(a) : __ldg(a);
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      float xv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xv[d] = x[vix<RM>(r, d, nb, np)];
+#pragma unroll
+      for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj) y[r * 3 + fi] = fmaf(K[fi * 3 + fj], xv[fj], y[r * 3 + fi]);
+    }
+  }
+}
+
+// Galerkin coarse operator of level lf + 1 from level lf: thread (S, I) forms the 3x3 block of coarse node I
+// toward coarse neighbour J = I + offset(S):
+//   A_c[I][S] = sum_{a, o} P[i][I] A[i][o] P[j][J],  i = 2I + a, j = i + o,  a, o in {-1, 0, 1}^3,
+// over fine interior i and j; P[i][I] = prod_d 2^-|a_d|, P[j][J] = prod_d 2^-|j_d - 2 J_d| (zero beyond 1).
+// Coarse boundary rows become identity rows; blocks toward coarse boundary nodes are zero.  The S = 13 thread
+// also writes the inverse diagonal.  The order of the additions is fixed.
+__global__ void __launch_bounds__(kMgBlock) k_mg_rap(MeshDev mf, MeshDev mc, const Inst *insts, const int *list,
+                                                     int lf) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const float *__restrict__ Af = (lf == 0) ? I.vals32 : I.mg->lv[lf].vals;
+  const MgLevel &C = I.mg->lv[lf + 1];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 27 * mc.nn) return;
+  const int S = t / mc.nn, ic = t - S * mc.nn;
+  int X, Y, Z;
+  const bool cb = on_boundary(mc, ic, X, Y, Z);
+  const int SX = S % 3 - 1, SY = (S / 3) % 3 - 1, SZ = S / 9 - 1;
+  const int JX = X + SX, JY = Y + SY, JZ = Z + SZ;
+  const bool jb = JX <= 0 || JY <= 0 || JZ <= 0 || JX >= mc.nx - 1 || JY >= mc.ny - 1 || JZ >= mc.nz - 1;
+  float acc[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] = 0.f;
+  if (!cb && !jb) {
+    const size_t npf = mf.np;
+#pragma unroll 1
+    for (int az = -1; az <= 1; ++az) {
+      const int iz = 2 * Z + az;
+      if (iz <= 0 || iz >= mf.nz - 1) continue;
+#pragma unroll 1
+      for (int ay = -1; ay <= 1; ++ay) {
+        const int iy = 2 * Y + ay;
+        if (iy <= 0 || iy >= mf.ny - 1) continue;
+#pragma unroll 1
+        for (int ax = -1; ax <= 1; ++ax) {
+          const int ix = 2 * X + ax;
+          if (ix <= 0 || ix >= mf.nx - 1) continue;
+          const float wi = half_pow(ax) * half_pow(ay) * half_pow(az);
+          const int i = (iz * mf.ny + iy) * mf.nx + ix;
+#pragma unroll 1
+          for (int oz = -1; oz <= 1; ++oz) {
+            const int jz = iz + oz, ez = jz - 2 * JZ;
+            if (ez < -1 || ez > 1 || jz <= 0 || jz >= mf.nz - 1) continue;
+#pragma unroll 1
+            for (int oy = -1; oy <= 1; ++oy) {
+              const int jy = iy + oy, ey = jy - 2 * JY;
+              if (ey < -1 || ey > 1 || jy <= 0 || jy >= mf.ny - 1) continue;
+#pragma unroll
+              for (int ox = -1; ox <= 1; ++ox) {
+                const int jx = ix + ox, ex = jx - 2 * JX;
+                if (ex < -1 || ex > 1 || jx <= 0 || jx >= mf.nx - 1) continue;
+                const float w = wi * half_pow(ex) * half_pow(ey) * half_pow(ez);
+                const int sf = (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1);
+#pragma unroll
+                for (int q = 0; q < 9; ++q) acc[q] = fmaf(w, __ldg(Af + (size_t)(sf * 9 + q) * npf + i), acc[q]);
+              }
+            }
+          }
+        }
+      }
+    }
+  } else if (cb && S == 13) {
+    acc[0] = acc[4] = acc[8] = 1.f;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) C.vals[(size_t)(S * 9 + q) * mc.np + ic] = acc[q];
+  if (S == 13)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) C.kinv[(size_t)ic * 3 + d] = cb ? 1.f : 1.f / acc[d * 4];
+}
+
+// t_l = b_l - A_l x_l (zero on boundary nodes).
+template <int NR, bool RM, bool STREAM>
+__global__ void __launch_bounds__(kMgBlock) k_mg_resid(MeshDev m, const Inst *insts, const int *list, int l) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const LvView v = view<NR>(I, l);
+  const size_t np = m.np;
+  int i, j, k;
+  if (on_boundary(m, n, i, j, k)) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v.t[vix<RM>(r, d, n, np)] = 0.f;
+    return;
+  }
+  float y[NR * 3];
+  apply_node<NR, RM, STREAM>(m, v.vals, v.x, n, y);
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const size_t q = vix<RM>(r, d, n, np);
+      v.t[q] = v.b[q] - y[r * 3 + d];
+    }
+}
+
+// b_{l+1} = P^T t_l; x_{l+1} = w D^-1 b_{l+1} (zero on coarse boundary nodes).  One thread per coarse node.
+template <int NR, bool RMF>
+__global__ void __launch_bounds__(kMgBlock) k_mg_restrict(MeshDev mf, MeshDev mc, const Inst *insts, const int *list,
+                                                          int lf, float omega) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= mc.nn) return;
+  const LvView f = view<NR>(I, lf);
+  const MgLevel &C = I.mg->lv[lf + 1];
+  const size_t npc = mc.np, npf = mf.np;
+  int X, Y, Z;
+  if (on_boundary(mc, ic, X, Y, Z)) {
+#pragma unroll
+    for (int c = 0; c < NR * 3; ++c) {
+      C.b[(size_t)c * npc + ic] = 0.f;
+      C.x[(size_t)c * npc + ic] = 0.f;
+    }
+    return;
+  }
+  float acc[NR * 3];
+#pragma unroll
+  for (int c = 0; c < NR * 3; ++c) acc[c] = 0.f;
+#pragma unroll 1
+  for (int a = 0; a < 27; ++a) {
+    const int ax = a % 3 - 1, ay = (a / 3) % 3 - 1, az = a / 9 - 1;
+    const int i = ((2 * Z + az) * mf.ny + (2 * Y + ay)) * mf.nx + (2 * X + ax);
+    const float w = half_pow(ax) * half_pow(ay) * half_pow(az);
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) acc[r * 3 + d] = fmaf(w, f.t[vix<RMF>(r, d, i, npf)], acc[r * 3 + d]);
+  }
+  float kd[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) kd[d] = C.kinv[(size_t)ic * 3 + d];
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const size_t q = (size_t)(r * 3 + d) * npc + ic;
+      C.b[q] = acc[r * 3 + d];
+      C.x[q] = omega * kd[d] * acc[r * 3 + d];
+    }
+}
+
+// t_l = x_l + P x_{l+1} on interior fine nodes (zero on boundary nodes).
+template <int NR, bool RMF>
+__global__ void __launch_bounds__(kMgBlock) k_mg_prolong(MeshDev mf, MeshDev mc, const Inst *insts, const int *list,
+                                                         int lf) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= mf.nn) return;
+  const LvView f = view<NR>(I, lf);
+  const float *__restrict__ xc = I.mg->lv[lf + 1].x;
+  const size_t npf = mf.np, npc = mc.np;
+  int i, j, k;
+  if (on_boundary(mf, n, i, j, k)) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) f.t[vix<RMF>(r, d, n, npf)] = 0.f;
+    return;
+  }
+  // coarse parents along each axis: even index -> (i / 2, 1); odd -> ((i - 1) / 2, 1/2), ((i + 1) / 2, 1/2)
+  const int px0 = i >> 1, px1 = (i + 1) >> 1, py0 = j >> 1, py1 = (j + 1) >> 1, pz0 = k >> 1, pz1 = (k + 1) >> 1;
+  const float wx = (i & 1) ? 0.5f : 1.f, wy = (j & 1) ? 0.5f : 1.f, wz = (k & 1) ? 0.5f : 1.f;
+  const int nxo = (i & 1) ? 2 : 1, nyo = (j & 1) ? 2 : 1, nzo = (k & 1) ? 2 : 1;
+  float acc[NR * 3];
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc[r * 3 + d] = f.x[vix<RMF>(r, d, n, npf)];
+  for (int cz = 0; cz < nzo; ++cz)
+    for (int cy = 0; cy < nyo; ++cy)
+      for (int cx = 0; cx < nxo; ++cx) {
+        const int J = ((cz ? pz1 : pz0) * mc.ny + (cy ? py1 : py0)) * mc.nx + (cx ? px1 : px0);
+        const float w = wx * wy * wz;
+#pragma unroll
+        for (int c = 0; c < NR * 3; ++c) acc[c] = fmaf(w, xc[(size_t)c * npc + J], acc[c]);
+      }
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f.t[vix<RMF>(r, d, n, npf)] = acc[r * 3 + d];
+}
+
+// out = in + w D^-1 (b - A in) on level l >= 1 (zero on boundary nodes); in/out select x, y or t.
+template <int NR>
+__global__ void __launch_bounds__(kMgBlock) k_mg_jacobi(MeshDev m, const Inst *insts, const int *list, int l,
+                                                        int src, int dst, float omega) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const LvView v = view<NR>(I, l);
+  const float *__restrict__ in = pick(v, src);
+  float *__restrict__ out = pick(v, dst);
+  const size_t np = m.np;
+  int i, j, k;
+  if (on_boundary(m, n, i, j, k)) {
+#pragma unroll
+    for (int c = 0; c < NR * 3; ++c) out[(size_t)c * np + n] = 0.f;
+    return;
+  }
+  float y[NR * 3];
+  apply_node<NR, false, false>(m, v.vals, in, n, y);
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const size_t q = (size_t)(r * 3 + d) * np + n;
+      out[q] = fmaf(omega * v.kinv[(size_t)n * 3 + d], v.b[q] - y[r * 3 + d], in[q]);
+    }
+}
+
+// Level-0 post-smoother and the CG scalars: z = t0 + w D^-1 (r - A t0), rz_i = sum r.z.  setup: p = z and
+// rz = rz_i (start of a solve); otherwise beta = rz_i / rz, rz = rz_i (right-hand sides still iterating).
+template <int NR, bool RM>
+__global__ void __launch_bounds__(kMgBlock) k_mg_post0(MeshDev m, const Inst *insts, const int *list, float omega,
+                                                       int setup) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  float acc[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) acc[r] = 0.f;
+  if (n < m.nn) {
+    const LvView v = view<NR>(I, 0);
+    float *__restrict__ p = NR == 1 ? I.p32 : I.P6;
+    const size_t np = m.np;
+    int i, j, k;
+    const bool bn = on_boundary(m, n, i, j, k);
+    float y[NR * 3];
+    if (!bn) apply_node<NR, RM, true>(m, v.vals, v.t, n, y);
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const size_t q = vix<RM>(r, d, n, np);
+        const float rv = v.b[q];
+        const float z = bn ? 0.f : fmaf(omega * v.kinv[(size_t)n * 3 + d], rv - y[r * 3 + d], v.t[q]);
+        v.x[q] = z;
+        if (setup) p[q] = z;
+        acc[r] = fmaf(rv, z, acc[r]);
+      }
+  }
+  double tot[NR];
+  if (grid_sum_f<NR>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+    if (NR == 1) {
+      CgState *c = I.cg;
+      if (!setup) c->beta = tot[0] / c->rz;
+      c->rz = tot[0];
+      if (!isfinite(tot[0])) {
+        c->done = 1;
+        I.out->nonfinite = 1;
+        I.out->cg_its = c->its;
+      }
+    } else {
+      Cg6State *c = I.cg6;
+      for (int r = 0; r < NR; ++r) {
+        if (c->done[r]) continue;
+        if (!setup) c->beta[r] = tot[r] / c->rz[r];
+        c->rz[r] = tot[r];
+        if (!isfinite(tot[r])) c->done[r] = 1;
+      }
+      int all = 1;
+      for (int r = 0; r < NR; ++r) all &= c->done[r];
+      c->all_done = all;
+      if (all) I.out->cg6_its = c->its;
+    }
+  }
+}
+
+inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+int mgb_launch_mg_rap(const MeshDev *mf, const MeshDev *mc, const Inst *insts, const int *list, int nlist, int lf,
+                      cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_mg_rap<<<dim3(cdiv((size_t)27 * mc->nn, kMgBlock), nlist), kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_resid(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l,
+                        cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const dim3 g(cdiv(m->nn, kMgBlock), nlist);
+  if (nr == 1) {
+    if (l == 0)
+      k_mg_resid<1, true, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+    else
+      k_mg_resid<1, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+  } else {
+    if (l == 0)
+      k_mg_resid<6, false, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+    else
+      k_mg_resid<6, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+  }
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_restrict(const MeshDev *mf, const MeshDev *mc, const Inst *insts, const int *list, int nlist,
+                           int nr, int lf, float omega, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const dim3 g(cdiv(mc->nn, kMgBlock), nlist);
+  if (nr == 1) {
+    if (lf == 0)
+      k_mg_restrict<1, true><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf, omega);
+    else
+      k_mg_restrict<1, false><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf, omega);
+  } else {
+    k_mg_restrict<6, false><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf, omega);
+  }
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_prolong(const MeshDev *mf, const MeshDev *mc, const Inst *insts, const int *list, int nlist,
+                          int nr, int lf, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const dim3 g(cdiv(mf->nn, kMgBlock), nlist);
+  if (nr == 1) {
+    if (lf == 0)
+      k_mg_prolong<1, true><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+    else
+      k_mg_prolong<1, false><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+  } else {
+    k_mg_prolong<6, false><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+  }
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_jacobi(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l, int src,
+                         int dst, float omega, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  if (l < 1 || src < 0 || src > 2 || dst < 0 || dst > 2 || src == dst) return (int)cudaErrorInvalidValue;
+  const dim3 g(cdiv(m->nn, kMgBlock), nlist);
+  if (nr == 1)
+    k_mg_jacobi<1><<<g, kMgBlock, 0, s>>>(*m, insts, list, l, src, dst, omega);
+  else
+    k_mg_jacobi<6><<<g, kMgBlock, 0, s>>>(*m, insts, list, l, src, dst, omega);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_post0(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, float omega,
+                        int setup, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const dim3 g(cdiv(m->nn, kMgBlock), nlist);
+  if (nr == 1)
+    k_mg_post0<1, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
+  else
+    k_mg_post0<6, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
+  return (int)cudaGetLastError();
+}
+
+}  // extern "C"

@@ -294,6 +294,11 @@ void micropp3_get_ctan_lin(const struct micropp3 *self, double *out36) {
   if (Engine *e = eng(self, "micropp3_get_ctan_lin")) guard("micropp3_get_ctan_lin", [&] { e->get_ctan_lin(out36); });
 }
 
+int micropp3_get_mg_levels(const struct micropp3 *self) {
+  Engine *e = eng(self, "micropp3_get_mg_levels");
+  return e ? e->mg_levels() : 0;
+}
+
 double micropp3_last_homogenize_ms(const struct micropp3 *self) {
   Engine *e = eng(self, "micropp3_last_homogenize_ms");
   return e ? e->last_homogenize_ms() : 0.0;

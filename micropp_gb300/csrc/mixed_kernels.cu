@@ -58,7 +58,11 @@ constexpr int kSpmvNodes = 4;       // FP32 SpMV: consecutive nodes per thread (
 // by the engine's autotuner.
 constexpr int kSpmv6Nodes = 2;      // 6-RHS SpMV: consecutive nodes per thread (one 8-byte load per entry)
 
-__global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list) {
+// zscale: 1 for Jacobi-preconditioned CG; the multigrid weight w when a V-cycle follows (z = w D^-1 r is then
+// its pre-smoothed level-0 iterate, and the V-cycle's last kernel sets p and rz).  ||D^-1 r|| stays the norm of
+// the stop test either way.
+__global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list,
+                                                           float zscale) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   float acc[2] = {0.f, 0.f};
@@ -77,14 +81,15 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
       const int row = n * 3 + d;
       const float kd = b ? 1.0f : 1.0f / vals[ell32_diag(m, n, d)];
       const float r = (float)bb[row];
-      const float z = kd * r;
+      const float zj = kd * r;
+      const float z = zscale * zj;
       kinv[row] = kd;
       du[row] = 0.0f;
       rv[row] = r;
       zv[row] = z;
       pv[row] = z;
       acc[0] = fmaf(r, z, acc[0]);
-      acc[1] = fmaf(z, z, acc[1]);
+      acc[1] = fmaf(zj, zj, acc[1]);
     }
   }
   double tot[2];
@@ -180,11 +185,15 @@ __global__ void __launch_bounds__(B) k_cg32_spmv(MeshDev m, const Inst *insts, c
 
 // du += alpha p; r -= alpha Ap; z = kinv r, kRowsPerThread rows per thread (loads of all rows first); the
 // last block sets beta, the norms and the stop flag.
-__global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Inst *insts, const int *list) {
+// mg: a V-cycle follows; z = w D^-1 r (its pre-smoothed level-0 iterate) and beta, rz are left to the V-cycle's
+// last kernel.  The stop test uses ||D^-1 r|| in both cases.
+__global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Inst *insts, const int *list, int mg,
+                                                            float omega) {
   const Inst &I = insts[list[blockIdx.y]];
   const CgState *cs = I.cg;
   if (cs->done) return;
   const float alpha = (float)cs->alpha;
+  const float zscale = mg ? omega : 1.0f;
   const int nrow = m.nn * 3;
   float *__restrict__ du = I.du32;
   float *__restrict__ rv = I.r32;
@@ -209,10 +218,11 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Ins
       if (row < nrow) {
         du[row] = fmaf(alpha, pv[q], dv[q]);
         const float r = fmaf(-alpha, av[q], rr[q]);
-        const float z = kv[q] * r;
+        const float zj = kv[q] * r;
+        const float z = zscale * zj;
         rv[row] = r;
         zv[row] = z;
-        acc[0] = fmaf(z, z, acc[0]);
+        acc[0] = fmaf(zj, zj, acc[0]);
         acc[1] = fmaf(r, z, acc[1]);
       }
     }
@@ -221,8 +231,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Ins
   if (grid_sum_f<2>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     CgState *c = I.cg;
     c->pnorm = sqrt(tot[0]);
-    c->beta = tot[1] / c->rz;
-    c->rz = tot[1];
+    if (!mg) {
+      c->beta = tot[1] / c->rz;
+      c->rz = tot[1];
+    }
     c->its += 1;
     c->done = !(c->its < c->max_its) || c->pnorm < c->min_err || c->pnorm < c->pnorm0 * c->rel_err;
     if (!isfinite(tot[0]) || !isfinite(tot[1])) {
@@ -337,8 +349,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
 // Refinement residual RF = F - K X (FP64 accumulation), start of a 6-RHS CG on it:
 // R = RF (FP32), D = 0, Z = kinv R, P = Z; the last block initialises the six CG states.  x_zero: X is
 // still 0 (the first sweep), RF = F without the product.
+// zscale as in k_cg32_setup.
 __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Inst *insts, const int *list,
-                                                            int x_zero) {
+                                                            int x_zero, float zscale) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[18];
@@ -381,13 +394,14 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
       for (int d = 0; d < 3; ++d) {
         const size_t idx = c6(r, d, np) + n;
         const float rr = (float)rf[r][d];
-        const float z = kd[d] * rr;
+        const float zj = kd[d] * rr;
+        const float z = zscale * zj;
         R6[idx] = rr;
         Z6[idx] = z;
         P6[idx] = z;
         D6[idx] = 0.0f;
         acc[r] += (double)rr * (double)z;
-        acc[6 + r] += (double)z * (double)z;
+        acc[6 + r] += (double)zj * (double)zj;
         acc[12 + r] += rf[r][d] * rf[r][d];
       }
   }
@@ -502,10 +516,13 @@ constexpr int kVec6Chunk = kVec6PerThread * kNodeBlock;
 // D += alpha P; R -= alpha AP; Z = kinv R for the right-hand sides still iterating.  A block takes one node
 // chunk through the 18 components in turn (the 16 loads of a component in flight together); an instance has
 // nn / kVec6Chunk blocks to reduce, and the last one sets beta_i and the stop flags.
-__global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list) {
+// mg as in k_cg32_update.
+__global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list, int mg,
+                                                           float omega) {
   const Inst &I = insts[list[blockIdx.y]];
   const Cg6State *cs = I.cg6;
   if (cs->all_done) return;
+  const float zscale = mg ? omega : 1.0f;
   float alpha[6];
   bool live[6];
 #pragma unroll
@@ -550,10 +567,11 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
         if (n < m.nn) {
           D6[n] = fmaf(alpha[r], pv[q], dv[q]);
           const float rr = fmaf(-alpha[r], av[q], rv[q]);
-          const float z = kd[q][d] * rr;
+          const float zj = kd[q][d] * rr;
+          const float z = zscale * zj;
           R6[n] = rr;
           Z6[n] = z;
-          acc[r] = fmaf(z, z, acc[r]);
+          acc[r] = fmaf(zj, zj, acc[r]);
           acc[6 + r] = fmaf(rr, z, acc[6 + r]);
         }
       }
@@ -567,8 +585,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
     for (int r = 0; r < 6; ++r) {
       if (!c->done[r]) {
         c->pnorm[r] = sqrt(tot[r]);
-        c->beta[r] = tot[6 + r] / c->rz[r];
-        c->rz[r] = tot[6 + r];
+        if (!mg) {
+          c->beta[r] = tot[6 + r] / c->rz[r];
+          c->rz[r] = tot[6 + r];
+        }
         c->done[r] = !(c->its < c->max_its) || c->pnorm[r] < c->min_err || c->pnorm[r] < c->pnorm0[r] * c->rel_err ||
                      !isfinite(tot[r]);
       }
@@ -787,9 +807,10 @@ static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) 
 
 extern "C" {
 
-int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, int nlist, float zscale,
+                          cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_setup<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg32_setup<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, zscale);
   return (int)cudaGetLastError();
 }
 
@@ -806,10 +827,11 @@ int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, i
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg32_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_cg32_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, float omega,
+                           cudaStream_t s) {
   if (nlist <= 0) return 0;
   const unsigned g = cdiv((size_t)m->nn * 3, (size_t)kRowsPerThread * kNodeBlock);
-  k_cg32_update<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg32_update<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg, omega);
   return (int)cudaGetLastError();
 }
 
@@ -840,10 +862,10 @@ int mgb_launch_t6_rhs(const MeshDev *m, const Inst *insts, const int *list, int 
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, int x_zero,
+int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, int x_zero, float zscale,
                            cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, x_zero);
+  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, x_zero, zscale);
   return (int)cudaGetLastError();
 }
 
@@ -859,9 +881,10 @@ int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, in
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, float omega,
+                          cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_update<<<dim3(cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_cg6_update<<<dim3(cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg, omega);
   return (int)cudaGetLastError();
 }
 
