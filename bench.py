@@ -8,7 +8,8 @@ RVE to half its target and accepts the step; a bench step is one macro iteration
 (stress and ctan) at its target strain through the public C ABI.  Inputs are synthetic.
 
 Two forms are measured on the same workload, one after the other (FORMS below):
-  fast  -- FP32 Jacobian and CG inside FP64 refinement, ctan by implicit differentiation (headline `value`);
+  fast  -- FP32 Jacobian and multigrid-preconditioned CG inside FP64 refinement, ctan by implicit
+           differentiation (headline `value`);
   plain -- the reference algorithm in FP64 (Newton + DPCG at the reference's tolerances, ctan from six
            perturbed Newton solves), the drop-in form.
 `value` is device-timed throughput (CUDA events on the handles' streams); `e2e` the wall-clock throughput of
@@ -81,14 +82,19 @@ def workload(n, rves, seed, rank):
 # The two forms.  plain: the reference algorithm in FP64 (Newton to the reference's tolerances, ctan from six
 # perturbed Newton solves).  fast: FP32 Jacobian and CG inside FP64 refinement, Newton converged to 1e-8 of the
 # initial residual (average stress within 1e-7 of the converged FP64 solution), ctan by implicit
-# differentiation (one 6-RHS tangent solve).
+# differentiation (one 6-RHS tangent solve), both FP32 solves preconditioned by a geometric multigrid V-cycle.
+# fast_jacobi (not in the default run): the same with the Jacobi preconditioner.
 # `batched`: all RVEs are Gauss points of one handle, homogenized together by one micropp3_homogenize call
 # (lockstep Newton and CG over the batch with per-RVE convergence masks); otherwise each RVE has its own
 # handle and they are homogenized one after the other, as a macro code calls one micro point at a time.
-# plain_batched (not in the default run) is the plain algorithm with batching alone.
+# plain_batched (not in the default run) is the plain algorithm with batching alone.  The mixed-size workload
+# was measured with fast_jacobi (--workload mixed --forms fast_jacobi,plain).
 FORMS = {
     "plain": dict(batched=False, cfg=dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5)),
-    "fast": dict(batched=True, cfg=dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8)),
+    "fast": dict(batched=True, cfg=dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8,
+                                        precond=1)),
+    "fast_jacobi": dict(batched=True, cfg=dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30,
+                                               nr_rel_tol=1e-8, precond=0)),
     "plain_batched": dict(batched=True, cfg=dict(precision=0, ctan_mode=0, nr_max_its=12, nr_max_tol=1e-5)),
 }
 

@@ -37,11 +37,11 @@ enum {
 /* Preconditioner of the FP32 CG solves (the mixed form's Newton corrections and the implicit ctan's 6-RHS
  * tangent solve). */
 enum {
-  MICROPP3_PRECOND_AUTO = 0,   /* multigrid where the grid coarsens (at least 4 elements along every axis and
-                                * more than 4 along one), Jacobi otherwise */
-  MICROPP3_PRECOND_JACOBI = 1, /* point Jacobi, as the reference's DPCG */
-  MICROPP3_PRECOND_MG = 2      /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
-                                * damped-Jacobi smoothing; every axis coarsens to ceil(elements / 2) */
+  MICROPP3_PRECOND_JACOBI = 0, /* point Jacobi, as the reference's DPCG (default) */
+  MICROPP3_PRECOND_MG = 1      /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
+                                * damped-Jacobi smoothing; every axis coarsens to ceil(elements / 2).  Needs at
+                                * least 4 elements along every axis and more than 4 along one.  On strongly
+                                * softened damage tangents its CG can stall where Jacobi's converges. */
 };
 
 /* Per-RVE status word of the last homogenize(). */

@@ -95,8 +95,8 @@ Engine::Engine(const micropp3_config &cfg) {
   // elements and some axis has more than 4.
   {
     const int pc = cfg.precond;
-    if (pc != MICROPP3_PRECOND_AUTO && pc != MICROPP3_PRECOND_JACOBI && pc != MICROPP3_PRECOND_MG)
-      throw std::invalid_argument("precond must be MICROPP3_PRECOND_AUTO, _JACOBI or _MG");
+    if (pc != MICROPP3_PRECOND_JACOBI && pc != MICROPP3_PRECOND_MG)
+      throw std::invalid_argument("precond must be MICROPP3_PRECOND_JACOBI or MICROPP3_PRECOND_MG");
     const bool fp32_solves = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
     if (pc == MICROPP3_PRECOND_MG && !fp32_solves)
       throw std::invalid_argument("the multigrid preconditioner applies to the FP32 solves (MICROPP3_MIXED or "
@@ -120,7 +120,7 @@ Engine::Engine(const micropp3_config &cfg) {
       c.np = (c.nn + 31) / 32 * 32;
       mg_mesh_.push_back(c);
     }
-    mg_ = fp32_solves && pc != MICROPP3_PRECOND_JACOBI && mg_mesh_.size() >= 2;
+    mg_ = pc == MICROPP3_PRECOND_MG && mg_mesh_.size() >= 2;
     if (pc == MICROPP3_PRECOND_MG && !mg_)
       throw std::invalid_argument("the multigrid preconditioner needs at least 4 elements along every axis and "
                                   "more than 4 along one");

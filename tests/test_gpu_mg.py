@@ -1,9 +1,9 @@
 """Multigrid preconditioner of the fast form's FP32 solves (Newton corrections and the 6-RHS tangent solve).
 
 The preconditioner changes how many CG iterations a solve takes, not what it converges to: the fast form with
-multigrid must meet the same bars against the tightly converged FP64 oracle as with Jacobi (average stress
-within 1e-7, ctan within 1e-5 of the oracle's central difference), with far fewer CG iterations.  Grids with
-an odd number of elements or different counts per axis coarsen to ceil(n / 2) per axis.
+multigrid (precond = MICROPP3_PRECOND_MG) must meet the same bars against the tightly converged FP64 oracle as
+with Jacobi (average stress within 1e-7, ctan within 1e-5 of the oracle's central difference), with fewer CG
+iterations.  Grids with an odd number of elements or different counts per axis coarsen to ceil(n / 2) per axis.
 """
 import numpy as np
 import pytest
@@ -20,22 +20,23 @@ SPHERE_DAMAGE = dict(micro_type=1, geo=(0.2, 0, 0, 0),
                      coupling=[2], lin_stress=0)
 
 
-@pytest.mark.parametrize("n,levels", [(4, 0), (5, 2), (10, 3), ((13, 6, 9), 2), ((3, 8, 8), 0), (60, 5)])
+@pytest.mark.parametrize("n,levels", [(5, 2), (10, 3), ((13, 6, 9), 2), (60, 5)])
 def test_levels(gpu_lib, n, levels):
     import micropp_gb300 as mg
-    g = mg.Micropp(gpu_config(n, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, calc_ctan_lin=0))
+    g = mg.Micropp(gpu_config(n, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, calc_ctan_lin=0,
+                              precond=mg.PRECOND_MG))
     assert g.mg_levels() == levels
-    j = mg.Micropp(gpu_config(n, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, calc_ctan_lin=0,
-                              precond=mg.PRECOND_JACOBI))
-    assert j.mg_levels() == 0
+    j = mg.Micropp(gpu_config(n, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, calc_ctan_lin=0))
+    assert j.mg_levels() == 0  # Jacobi is the default
 
 
 def test_rejected_configurations(gpu_lib):
     import micropp_gb300 as mg
     with pytest.raises(RuntimeError, match="FP32 solves"):
         mg.Micropp(gpu_config(6, precond=mg.PRECOND_MG))  # FP64 Newton and perturbation ctan: no FP32 solve
-    with pytest.raises(RuntimeError, match="4 elements"):
-        mg.Micropp(gpu_config((3, 8, 8), precision=mg.MIXED, precond=mg.PRECOND_MG))
+    for n in (4, (3, 8, 8)):
+        with pytest.raises(RuntimeError, match="4 elements"):
+            mg.Micropp(gpu_config(n, precision=mg.MIXED, precond=mg.PRECOND_MG))
     with pytest.raises(RuntimeError, match="precond"):
         mg.Micropp(gpu_config(6, precision=mg.MIXED, precond=7))
 
@@ -67,12 +68,13 @@ DAMAGE_PATH = [np.array([2e-2, -6e-3, 0, 1e-2, 0, 0]) * s / 2 for s in (1, 2)]
 
 
 def test_damage_layers_mg_against_jacobi(gpu_lib):
-    """Layered damage RVE of 20^3: both preconditioners meet the bars, multigrid with fewer CG iterations (the
-    gap grows with the grid: Jacobi-PCG iterations grow with n, the V-cycle's stay near 10 per solve)."""
+    """Layered damage RVE of 12^3: both preconditioners meet the bars, multigrid with fewer CG iterations.  The
+    gap grows with the grid (Jacobi-PCG iterations grow with n, the V-cycle's stay near 10 per solve): 2x here,
+    about 20x on 60^3 RVEs."""
     import micropp_gb300 as mg
-    its_mg, g = _fast_path(20, damage_kw(20), DAMAGE_PATH, mg.PRECOND_MG)
-    assert g.mg_levels() == 4
-    its_j, _ = _fast_path(20, damage_kw(20), DAMAGE_PATH, mg.PRECOND_JACOBI)
+    its_mg, g = _fast_path(12, damage_kw(12), DAMAGE_PATH, mg.PRECOND_MG)
+    assert g.mg_levels() == 3
+    its_j, _ = _fast_path(12, damage_kw(12), DAMAGE_PATH, mg.PRECOND_JACOBI)
     assert its_mg < 0.6 * its_j, (its_mg, its_j)
 
 
@@ -84,14 +86,18 @@ def test_odd_and_noncubic_grids(gpu_lib, n):
 
 
 def test_linear_ctan_mg(gpu_lib):
-    """The constructor's linear ctan through the multigrid tangent solve equals the oracle's (tight CG)."""
+    """The constructor's linear ctan through the multigrid tangent solve equals the oracle's (tight CG) and the
+    Jacobi form's: the refined solve does not depend on the preconditioner (measured on a GB300: 2.3e-8 from the
+    oracle with either).  On an 11^3 grid both reach only 3.2e-6, the rounding of the FP32 Jacobian."""
     import micropp_gb300 as mg
     kw = dict(micro_type=1, geo=(0.2, 0, 0, 0),
               mats=((0, 1e7, 0.25, 0, 0, 0), (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0)), coupling=[2])
-    g = mg.Micropp(gpu_config(11, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=mg.PRECOND_MG, **kw))
-    o = orc.OracleRVE(oracle_config(11, cg_rel_tol=1e-13, **kw))
+    g = mg.Micropp(gpu_config(10, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=mg.PRECOND_MG, **kw))
+    j = mg.Micropp(gpu_config(10, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, **kw))
+    o = orc.OracleRVE(oracle_config(10, cg_rel_tol=1e-13, **kw))
     assert g.mg_levels() == 3
     assert rel_err(g.ctan_lin(), o.ctan_lin()) < 1e-6
+    assert rel_err(g.ctan_lin(), j.ctan_lin()) < 1e-7
 
 
 def test_batched_mg_uneven_points(gpu_lib):
@@ -100,7 +106,8 @@ def test_batched_mg_uneven_points(gpu_lib):
     n = 10
     kw = damage_kw(n)
     kw["coupling"] = [2] * 4
-    g = mg.Micropp(gpu_config(n, ngp=4, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, **kw, **FAST))
+    g = mg.Micropp(gpu_config(n, ngp=4, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=mg.PRECOND_MG,
+                              **kw, **FAST))
     o = orc.OracleRVE(oracle_config(n, ngp=4, **kw, **TIGHT))
     assert g.mg_levels() == 3
     strains = [DAMAGE_PATH[1], 0.1 * DAMAGE_PATH[1], -DAMAGE_PATH[1], DAMAGE_PATH[0]]
