@@ -8,10 +8,10 @@ element phase maps (``micropp3_config.elem_type``), the way a caller of the libr
 * ``spheres(n, k, r, seed)`` -- k non-overlapping spheres of radius r with seeded uniform centres
   (rejection sampling, fully inside the cube), phase 1 inside.
 
-Material parameters follow the damage-law mapping recorded in the design doc: the reference damage law has a
-single threshold parameter Xt (material.cpp:227-268) and a hard-wired softening table, so the damage
-matrix uses Xt ~ U[1e5, 3e5] per RVE (smaller Xt fully damages Gauss points and the reference itself
-returns NaN stresses).
+Damage-law parameters: the reference damage law has a single threshold parameter Xt (material.cpp:227-268)
+and a softening table hard-wired to Ey = 1e5.  With Xt < 1e5 it fully damages Gauss points (the reference
+itself returns NaN stresses); with Xt > 1e5 the damaged stress jumps by q(r)/r at first loading.  The
+benchmark's damage matrix therefore uses Xt = 1e5, where the law is continuous.
 """
 import numpy as np
 
