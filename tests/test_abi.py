@@ -136,3 +136,26 @@ def test_product_never_reaches_the_oracle():
             p = os.path.join(ROOT, d, f)
             if os.path.isfile(p) and f.endswith((".py", ".cu", ".cuh", ".cpp", ".hpp", ".h", ".c")):
                 assert not pat.search(open(p).read()), p
+
+
+def test_ctypes_mirror_matches_c_layout(tmp_path):
+    """The Python ctypes structs used by the tests and the bench have the C headers' field offsets and sizes
+    (compiled with the host C compiler from include/)."""
+    import micropp_gb300 as mg
+    structs = [("struct micropp3_config", mg.Config, {}), ("struct material_base", mg.MaterialBase, {"lam": "lambda"})]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "micropp_gb300.h"', "int main(void) {"]
+    for cname, py, rename in structs:
+        lines.append(f'  printf("{cname}:sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname}:{f} %zu\\n", offsetof({cname}, {rename.get(f, f)}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                                check=True).stdout.splitlines())
+    for cname, py, _ in structs:
+        assert int(out[f"{cname}:sizeof"]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(out[f"{cname}:{f}"]) == getattr(py, f).offset, (cname, f)
