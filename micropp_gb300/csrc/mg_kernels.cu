@@ -9,8 +9,8 @@
 // A_c = P^T A P; with trilinear P and a 27-point operator it is again a 27-point operator of 3x3 blocks, so
 // every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].
 //
-// The preconditioner is one V-cycle with damped Jacobi (weight kMgOmega) as pre- and post-smoother and a
-// fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric operation, so the
+// The preconditioner is one V-cycle with damped Jacobi (weight w, passed by the host: 0.6) as pre- and
+// post-smoother and a fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric operation, so the
 // V-cycle is a fixed symmetric preconditioner and the CG recurrences stay those of preconditioned CG.
 //
 //   level 0:   x0 = w D^-1 r                    (written by the CG update kernel)
