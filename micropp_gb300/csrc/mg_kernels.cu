@@ -10,8 +10,9 @@
 // every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].
 //
 // The preconditioner is one V-cycle with damped Jacobi (weight w, passed by the host: 0.6) as pre- and
-// post-smoother and a fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric operation, so the
-// V-cycle is a fixed symmetric preconditioner and the CG recurrences stay those of preconditioned CG.
+// post-smoother and a fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric
+// operation, so the V-cycle is a fixed symmetric preconditioner and the CG recurrences stay those of
+// preconditioned CG.
 //
 //   level 0:   x0 = w D^-1 r                    (written by the CG update kernel)
 //   l < L-1:   t_l = b_l - A_l x_l;  b_{l+1} = P^T t_l;  x_{l+1} = w D^-1 b_{l+1}
