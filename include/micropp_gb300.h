@@ -41,7 +41,8 @@ enum {
   MICROPP3_PRECOND_MG = 1      /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
                                 * damped-Jacobi smoothing; every axis coarsens to ceil(elements / 2).  Needs at
                                 * least 4 elements along every axis and more than 4 along one.  On strongly
-                                * softened damage tangents its CG can stall where Jacobi's converges. */
+                                * anisotropic tangents (loading damage, J2 plastic flow) its CG can stall where
+                                * Jacobi's converges. */
 };
 
 /* Per-RVE status word of the last homogenize(). */
