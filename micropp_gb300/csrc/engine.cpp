@@ -39,11 +39,14 @@ constexpr int kTangentSweeps = 4;
 // Lowest relative tolerance asked of the mixed form's FP32 Newton CG.
 constexpr double kFp32CgFloor = 1.0e-6;
 
-// Multigrid preconditioner of the FP32 solves: damped-Jacobi weight of the smoothers, pairs of Jacobi sweeps
-// on the coarsest level after the first one (9 sweeps), CG iterations between polls of the active count.
+// Multigrid preconditioner of the FP32 solves: the smoother diagonal max(a_ii / kMgOmega, kMgSafe sum_j |a_ij|),
+// pairs of Jacobi sweeps on the coarsest level after the first one (9 sweeps), CG iterations between polls of
+// the active count, and the iteration cap of a multigrid solve: one that reaches it is redone with Jacobi.
 constexpr float kMgOmega = 0.6f;
+constexpr float kMgSafe = 0.55f;
 constexpr int kMgCoarsePairs = 4;
 constexpr int kMgChunk = 4;
+constexpr int kMgMaxIts = 100;
 
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
@@ -443,7 +446,7 @@ double Engine::slot_bytes() const {
   if (precision_ == MICROPP3_MIXED) b += 4.0 * 5.0 * nd;
   if (ctan_mode_ == MICROPP3_CTAN_IMPLICIT) b += (8.0 * 2.0 + 4.0 * 5.0) * 18.0 * np;
   if (mg_) {
-    b += 4.0 * 18.0 * np;
+    b += 4.0 * 21.0 * np;
     for (size_t l = 1; l < mg_mesh_.size(); ++l) b += 4.0 * (kEllPerNode + 3.0 + 4.0 * 18.0) * mg_mesh_[l].np;
   }
   return b;
@@ -511,6 +514,7 @@ void Engine::ensure_slots(int n) {
         return p;
       };
       h.lv[0].t = buf((size_t)18 * mesh_.np, "multigrid level-0 residual");
+      h.lv[0].kinv = buf((size_t)3 * mesh_.np, "multigrid level-0 smoother diagonal");
       for (size_t l = 1; l < mg_mesh_.size(); ++l) {
         const size_t np = mg_mesh_[l].np;
         h.lv[l].vals = buf((size_t)kEllPerNode * np, "multigrid operator");
@@ -822,41 +826,38 @@ void Engine::cg_solve(const std::vector<int> &slots) {
 }
 
 // The mixed form's CG: FP32 values and vectors, FP64 dot products, same iteration and stop rule, with a
-// relative tolerance per slot.
-void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols) {
+// relative tolerance per slot.  use_mg: multigrid-preconditioned (when the handle has multigrid), capped at
+// kMgMaxIts iterations; otherwise Jacobi with cg_max_its.
+void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols, bool use_mg) {
   const int n = (int)slots.size();
+  const bool mg = mg_ && use_mg;
   for (int a = 0; a < n; ++a) {
     CgState c{};
     c.min_err = cg_abs_tol_;
     c.rel_err = rel_tols[a];
-    c.max_its = cg_max_its_;
+    c.max_its = mg ? std::min(cg_max_its_, kMgMaxIts) : cg_max_its_;
     check(cudaMemcpyAsync(slots_[slots[a]].cg, &c, sizeof(CgState), cudaMemcpyHostToDevice, stream_), "cg init");
   }
   launches_ += 1;
-  check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, mg_ ? kMgOmega : 1.0f, stream_), "cg32 setup");
-  if (mg_) {
-    mg_vcycle(1, n, true);
-  }
+  check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, mg ? 1 : 0, stream_), "cg32 setup");
+  if (mg) mg_vcycle(1, n, true);
   const int block = tuned_block(0, n);
   const double nrow = (double)nndim();
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 4);  // per iteration and instance, as in cg_solve
   const double upd_bytes = nrow * 11.0 * 4;
-  const int chunk = mg_ ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
+  const int chunk = mg ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
   int done_its = 0;
   while (done_its <= cg_max_its_) {
-    run_chunk(1, n, [&] {
+    run_chunk(mg ? 1 : 3, n, [&] {
       for (int it = 0; it < chunk; ++it) {
         if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
         timer_begin(t_spmv_, 0.0);
         check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, n, block, stream_), "cg32 spmv");
         timer_end(t_spmv_);
         timer_begin(t_update_, 0.0);
-        check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, mg_ ? 1 : 0, kMgOmega, stream_),
-                     "cg32 update");
+        check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, mg ? 1 : 0, stream_), "cg32 update");
         timer_end(t_update_);
-        if (mg_) {
-          mg_vcycle(1, n, false);
-        }
+        if (mg) mg_vcycle(1, n, false);
         timer_begin(t_update_, 0.0);
         check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
         timer_end(t_update_);
@@ -872,7 +873,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
     const double its = listed_cg_its(slots);
     timer_add_bytes(t_spmv_, its * spmv_bytes);
     timer_add_bytes(t_update_, its * upd_bytes);
-    if (mg_) {
+    if (mg) {
       timer_add_bytes(t_mg1_, (its + n) * mg_fine_bytes(1));
       timer_add_bytes(t_mgc_, (its + n) * mg_coarse_bytes(1));
     }
@@ -898,17 +899,26 @@ void Engine::assemble32(int nlist) {
   if (mg_) mg_rap(nlist);
 }
 
-// Galerkin operators P^T A P of every coarse level, finest first.  Algorithmic bytes: each level's operator
-// read once and the next one written once.
+// Galerkin operators P^T A P of every coarse level, finest first, and the safeguarded smoother diagonal of
+// every level.  Algorithmic bytes: each level's operator read twice (product, diagonal) and the next one written
+// once.
 void Engine::mg_rap(int nlist) {
   double bytes = 0.0;
-  for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l)
-    bytes += 4.0 * kEllPerNode * (double)(mg_mesh_[l].np + mg_mesh_[l + 1].np);
+  for (size_t l = 0; l < mg_mesh_.size(); ++l) {
+    bytes += 4.0 * kEllPerNode * (double)mg_mesh_[l].np;
+    if (l + 1 < mg_mesh_.size()) bytes += 4.0 * kEllPerNode * (double)(mg_mesh_[l].np + mg_mesh_[l + 1].np);
+  }
   timer_begin(t_asm_, nlist * bytes);
+  launches_ += 1;
+  check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
+               "multigrid smoother diagonal");
   for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l) {
-    launches_ += 1;
+    launches_ += 2;
     check_launch(mgb_launch_mg_rap(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, (int)l, stream_),
                  "multigrid Galerkin operator");
+    check_launch(mgb_launch_mg_sdiag(&mg_mesh_[l + 1], d_insts_, d_list_, nlist, (int)l + 1, kMgOmega, kMgSafe,
+                                     stream_),
+                 "multigrid smoother diagonal");
   }
   timer_end(t_asm_);
 }
@@ -947,26 +957,26 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup) {
       timer_end(fine);
       timer_begin(t_mgc_, 0.0);
     }
-    check_launch(mgb_launch_mg_restrict(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, kMgOmega,
+    check_launch(mgb_launch_mg_restrict(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, 1.0f,
                                         stream_),
                  "multigrid restriction");
   }
   for (int k = 0; k < kMgCoarsePairs; ++k) {
-    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 0, 1, kMgOmega, stream_),
+    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 0, 1, 1.0f, stream_),
                  "multigrid coarse sweep");
-    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 1, 0, kMgOmega, stream_),
+    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 1, 0, 1.0f, stream_),
                  "multigrid coarse sweep");
   }
   for (int l = L - 2; l >= 0; --l) {
     check_launch(mgb_launch_mg_prolong(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, stream_),
                  "multigrid prolongation");
     if (l > 0)
-      check_launch(mgb_launch_mg_jacobi(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, 2, 0, kMgOmega, stream_),
+      check_launch(mgb_launch_mg_jacobi(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, 2, 0, 1.0f, stream_),
                    "multigrid post-smoother");
   }
   timer_end(t_mgc_);
   timer_begin(fine, 0.0);
-  check_launch(mgb_launch_mg_post0(&mesh_, d_insts_, d_list_, nlist, nr, kMgOmega, setup ? 1 : 0, stream_),
+  check_launch(mgb_launch_mg_post0(&mesh_, d_insts_, d_list_, nlist, nr, 1.0f, setup ? 1 : 0, stream_),
                "multigrid level-0 post-smoother");
   timer_end(fine);
   launches_ += 2 * (L - 1) + 2 * kMgCoarsePairs + (L - 1) + (L - 2) + 1;
@@ -975,8 +985,10 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup) {
 // Implicit ctan of the listed slots at their current u with their vars_old: assemble the FP32 tangent, form
 // the six right-hand sides, solve with refined FP32 CG sweeps, average.  out.ctan of each slot is valid
 // afterwards.  Returns the CG iterations each slot spent.
-std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
+std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_mg) {
   const int n = (int)slots.size();
+  const bool mg = mg_ && use_mg;
+  std::vector<char> mg_capped(n, 0);  // a multigrid sweep of the slot reached kMgMaxIts
   std::vector<int> its(n, 0);
   upload_insts();
   upload_list(slots);
@@ -988,7 +1000,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   // write D, R, Z; p-update: read Z, P, write P (per right-hand side).  Credited per instance iteration.
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 6 * 4);
   const double upd6_bytes = nrow * 6.0 * 10.0 * 4;
-  const int chunk = mg_ ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
+  const int chunk = mg ? kMgChunk : (mesh_.nn > 200000) ? 8 : 32;
   std::vector<int> live = slots;
   std::vector<int> live_idx(n);
   for (int i = 0; i < n; ++i) live_idx[i] = i;
@@ -997,13 +1009,13 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
       Cg6State c{};
       c.min_err = 0.0;
       c.rel_err = kTangentSweepRel;
-      c.max_its = cg_max_its_;
+      c.max_its = mg ? std::min(cg_max_its_, kMgMaxIts) : cg_max_its_;
       check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
     }
     if (sweep > 0) upload_list(live);
     launches_ += 1;
     check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
-                                        mg_ ? kMgOmega : 1.0f, stream_),
+                                        mg ? 1 : 0, stream_),
                  "tangent residual");
     download_out();
     std::vector<int> next, next_idx;
@@ -1026,34 +1038,29 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
         Cg6State c{};
         c.min_err = 0.0;
         c.rel_err = kTangentSweepRel;
-        c.max_its = cg_max_its_;
+        c.max_its = mg ? std::min(cg_max_its_, kMgMaxIts) : cg_max_its_;
         check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
       }
       launches_ += 1;
       check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
-                                          mg_ ? kMgOmega : 1.0f, stream_),
+                                          mg ? 1 : 0, stream_),
                    "tangent residual");
     }
     const int nl = (int)live.size();
-    if (mg_) {
-      mg_vcycle(6, nl, true);
-    }
+    if (mg) mg_vcycle(6, nl, true);
     const int block = tuned_block(1, nl);
     int done_its = 0;
     while (done_its <= cg_max_its_) {
-      run_chunk(2, nl, [&] {
+      run_chunk(mg ? 2 : 4, nl, [&] {
         for (int it = 0; it < chunk; ++it) {
           if (it == chunk - 1) check(cudaMemsetAsync(d_count_, 0, sizeof(unsigned int), stream_), "count reset");
           timer_begin(t_spmv6_, 0.0);
           check_launch(mgb_launch_cg6_spmv(&mesh_, d_insts_, d_list_, nl, block, stream_), "cg6 spmv");
           timer_end(t_spmv6_);
           timer_begin(t_upd6_, 0.0);
-          check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, mg_ ? 1 : 0, kMgOmega, stream_),
-                       "cg6 update");
+          check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, mg ? 1 : 0, stream_), "cg6 update");
           timer_end(t_upd6_);
-          if (mg_) {
-            mg_vcycle(6, nl, false);
-          }
+          if (mg) mg_vcycle(6, nl, false);
           timer_begin(t_upd6_, 0.0);
           check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
           timer_end(t_upd6_);
@@ -1073,7 +1080,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
       total_cg_its_ += h_out_[live[a]].cg6_its;
       timer_add_bytes(t_spmv6_, h_out_[live[a]].cg6_its * spmv_bytes);
       timer_add_bytes(t_upd6_, h_out_[live[a]].cg6_its * upd6_bytes);
-      if (mg_) {
+      if (mg && h_out_[live[a]].cg6_its >= std::min(cg_max_its_, kMgMaxIts)) mg_capped[live_idx[a]] = 1;
+      if (mg) {
         timer_add_bytes(t_mg6_, (h_out_[live[a]].cg6_its + 1) * mg_fine_bytes(6));
         timer_add_bytes(t_mgc_, (h_out_[live[a]].cg6_its + 1) * mg_coarse_bytes(6));
       }
@@ -1086,6 +1094,20 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots) {
   else
     check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
   download_out();
+  if (mg) {
+    // Slots whose multigrid sweeps reached the iteration cap are solved again with Jacobi, from the start.
+    std::vector<int> redo, redo_idx;
+    for (int i = 0; i < n; ++i)
+      if (mg_capped[i]) {
+        redo.push_back(slots[i]);
+        redo_idx.push_back(i);
+      }
+    if (!redo.empty()) {
+      const std::vector<int> its2 = tangent_solve(redo, false);
+      for (size_t a = 0; a < redo.size(); ++a) its[redo_idx[a]] += its2[a];
+      upload_list(slots);
+    }
+  }
   return its;
 }
 
@@ -1146,6 +1168,7 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     int bicg_its = 0;
     bool have_residual = false;
     bool a0_iteration = false;
+    std::vector<int> mg_its(na, 0);  // iterations of multigrid solves redone with Jacobi
     if (mixed) {
       assemble32(na);
     } else if (use_A0_ && !exact_tangent_ && res[idx[0]].its < its_with_A0_) {
@@ -1178,6 +1201,23 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
         eta[a] = std::max(floor, std::min(0.1, want));
       }
       cg_solve32(active, eta);
+      if (mg_) {
+        // A multigrid solve that reached its iteration cap is redone from du = 0 with Jacobi.
+        download_out();
+        std::vector<int> redo;
+        std::vector<double> redo_eta;
+        for (int a = 0; a < na; ++a)
+          if (h_out_[active[a]].cg_maxed) {
+            mg_its[a] = h_out_[active[a]].cg_its;
+            redo.push_back(active[a]);
+            redo_eta.push_back(eta[a]);
+          }
+        if (!redo.empty()) {
+          upload_list(redo);
+          cg_solve32(redo, redo_eta, false);
+          upload_list(active);
+        }
+      }
       launches_ += 1;
       check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
       residual(active);
@@ -1249,7 +1289,7 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     for (size_t a = 0; a < active.size(); ++a) {
       const int i = idx[a];
       const InstOut &o = h_out_[slots[i]];
-      const int its = (exact_tangent_ && !mixed) ? bicg_its : o.cg_its;
+      const int its = ((exact_tangent_ && !mixed) ? bicg_its : o.cg_its) + mg_its[a];
       res[i].solver_its += its;
       res[i].cg_maxed |= (exact_tangent_ && !mixed) ? !last_bicg_converged_ : o.cg_maxed != 0;
       total_cg_its_ += its;

@@ -170,8 +170,8 @@ class Engine {
   void download_out();
   void residual(const std::vector<int> &slots);
   void cg_solve(const std::vector<int> &slots);
-  void cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols);
-  std::vector<int> tangent_solve(const std::vector<int> &slots);
+  void cg_solve32(const std::vector<int> &slots, const std::vector<double> &rel_tols, bool use_mg = true);
+  std::vector<int> tangent_solve(const std::vector<int> &slots, bool use_mg = true);
   double slot_bytes() const;
   std::vector<NewtonResult> newton(const std::vector<int> &slots, const std::vector<std::array<double, 6>> &strains);
   void homogenize_fe_batch(const std::vector<int> &gp_ids);

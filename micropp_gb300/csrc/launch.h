@@ -42,26 +42,26 @@ int mgb_launch_assembly32(const mgb::MeshDev *m, const mgb::Mats *mats, const in
 int mgb_launch_assembly_gather32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *k0g,
                               const float *kesum, const float *dsh32, const mgb::Inst *insts, const int *list,
                               int nlist, cudaStream_t s);
-// zscale: 1 (Jacobi) or the multigrid weight (a V-cycle and mgb_launch_mg_post0 with setup = 1 follow).
-int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, float zscale,
+// mg = 1: a V-cycle and mgb_launch_mg_post0 with setup = 1 follow.
+int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int mg,
                           cudaStream_t s);
 // block: 64, 128 or 256 threads (any other value: 128).
 int mgb_launch_cg32_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int block,
                          cudaStream_t s);
 // mg = 1: a V-cycle and mgb_launch_mg_post0 follow (they set rz and beta).
 int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int mg,
-                           float omega, cudaStream_t s);
+                           cudaStream_t s);
 int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                             unsigned int *active_count, cudaStream_t s);
 int mgb_launch_add_du32(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_axpy_du32(const mgb::MeshDev *m, double *u, const float *du, double a, cudaStream_t s);
 int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
-                           float zscale, cudaStream_t s);
+                           int mg, cudaStream_t s);
 int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int block,
                         cudaStream_t s);
 int mgb_launch_cg6_update(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int mg,
-                          float omega, cudaStream_t s);
+                          cudaStream_t s);
 int mgb_launch_cg6_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                            unsigned int *active_count, cudaStream_t s);
 int mgb_launch_t6_accumulate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
@@ -78,6 +78,9 @@ int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8
 // 0 = x, 1 = y, 2 = t of level l >= 1.
 int mgb_launch_mg_rap(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,
                       int nlist, int lf, cudaStream_t s);
+// Inverse safeguarded smoother diagonal of level l: 1 / max(a_dd / omega, c sum_j |a_dj|).
+int mgb_launch_mg_sdiag(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int l,
+                        float omega, float c, cudaStream_t s);
 int mgb_launch_mg_resid(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
                         cudaStream_t s);
 int mgb_launch_mg_restrict(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,

@@ -9,16 +9,21 @@
 // A_c = P^T A P; with trilinear P and a 27-point operator it is again a 27-point operator of 3x3 blocks, so
 // every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].
 //
-// The preconditioner is one V-cycle with damped Jacobi (weight w, passed by the host: 0.6) as pre- and
-// post-smoother and a fixed number of Jacobi sweeps on the coarsest level.  Every step is a linear, symmetric
-// operation, so the V-cycle is a fixed symmetric preconditioner and the CG recurrences stay those of
-// preconditioned CG.
+// The preconditioner is one V-cycle with a damped-Jacobi smoother before and after the coarse correction and a
+// fixed number of Jacobi sweeps on the coarsest level.  The smoother's diagonal is safeguarded per row:
+// d_i = max(a_ii / w, c sum_j |a_ij|) with w = 0.6 and c > 1/2 (k_mg_sdiag).  It is the plain damped diagonal
+// wherever that contracts; where the operator is strongly anisotropic (loading damage tangents) the Gershgorin
+// bound takes over, since 2 D - A is then diagonally dominant and every sweep contracts for an SPD operator.
+// Every step is linear and symmetric, so the V-cycle is a fixed symmetric positive-definite preconditioner and
+// the CG recurrences stay those of preconditioned CG.
 //
-//   level 0:   x0 = w D^-1 r                    (written by the CG update kernel)
-//   l < L-1:   t_l = b_l - A_l x_l;  b_{l+1} = P^T t_l;  x_{l+1} = w D^-1 b_{l+1}
+//   level 0:   x0 = D^-1 r                      (written by the CG update kernel)
+//   l < L-1:   t_l = b_l - A_l x_l;  b_{l+1} = P^T t_l;  x_{l+1} = D^-1 b_{l+1}
 //   coarsest:  (sweeps - 1) x Jacobi sweeps, ping-pong between x and y
-//   l >= 1:    t_l = x_l + P x_{l+1};  x_l = t_l + w D^-1 (b_l - A_l t_l)
-//   level 0:   t_0 = x_0 + P x_1;  z = t_0 + w D^-1 (r - A t_0), with r.z and the CG scalars
+//   l >= 1:    t_l = x_l + P x_{l+1};  x_l = t_l + D^-1 (b_l - A_l t_l)
+//   level 0:   t_0 = x_0 + P x_1;  z = t_0 + D^-1 (r - A t_0), with r.z and the CG scalars
+// (D: the safeguarded smoother diagonal of each level; lv[l].kinv holds its inverse.  The kernels' omega
+// argument scales D^-1 and is 1 with it.)
 //
 // Level 0 vectors are the CG's own: node-interleaved r32/z32 for one right-hand side, component-major R6/Z6
 // for six; the level-0 residual and prolongation go to lv[0].t (3 * nn or 18 * np floats).  Every kernel
@@ -66,7 +71,7 @@ __device__ __forceinline__ LvView view(const Inst &I, int l) {
   LvView v;
   if (l == 0) {
     v.vals = I.vals32;
-    v.kinv = I.kinv32;
+    v.kinv = L.kinv;
     v.b = NR == 1 ? I.r32 : I.R6;
     v.x = NR == 1 ? I.z32 : I.Z6;
     v.y = nullptr;
@@ -117,8 +122,8 @@ __device__ __forceinline__ void apply_node(const MeshDev &m, const float *__rest
 // toward coarse neighbour J = I + offset(S):
 //   A_c[I][S] = sum_{a, o} P[i][I] A[i][o] P[j][J],  i = 2I + a, j = i + o,  a, o in {-1, 0, 1}^3,
 // over fine interior i and j; P[i][I] = prod_d 2^-|a_d|, P[j][J] = prod_d 2^-|j_d - 2 J_d| (zero beyond 1).
-// Coarse boundary rows become identity rows; blocks toward coarse boundary nodes are zero.  The S = 13 thread
-// also writes the inverse diagonal.  The order of the additions is fixed.
+// Coarse boundary rows become identity rows; blocks toward coarse boundary nodes are zero.  The order of the
+// additions is fixed.
 __global__ void __launch_bounds__(kMgBlock) k_mg_rap(MeshDev mf, MeshDev mc, const Inst *insts, const int *list,
                                                      int lf) {
   const Inst &I = insts[list[blockIdx.y]];
@@ -178,9 +183,42 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_rap(MeshDev mf, MeshDev mc, con
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) C.vals[(size_t)(S * 9 + q) * mc.np + ic] = acc[q];
-  if (S == 13)
+}
+
+// Inverse of the safeguarded smoother diagonal of level l, per row (n, d):
+//   1 / max(a_dd / omega, c * sum_j |a_dj|)
+// over the row's interior columns (boundary columns are eliminated by the Dirichlet rows; coarse operators hold
+// zeros there).  Boundary rows get 1.
+__global__ void __launch_bounds__(kMgBlock) k_mg_sdiag(MeshDev m, const Inst *insts, const int *list, int l,
+                                                       float omega, float c) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const float *__restrict__ vals = (l == 0) ? I.vals32 : I.mg->lv[l].vals;
+  float *__restrict__ kinv = I.mg->lv[l].kinv;
+  int i, j, k;
+  if (on_boundary(m, n, i, j, k)) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) C.kinv[(size_t)ic * 3 + d] = cb ? 1.f : 1.f / acc[d * 4];
+    for (int d = 0; d < 3; ++d) kinv[(size_t)n * 3 + d] = 1.f;
+    return;
+  }
+  const size_t np = m.np;
+  float l1[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int s = 0; s < 27; ++s) {
+    const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
+    int bi, bj, bk;
+    if (on_boundary(m, nb, bi, bj, bk)) continue;
+#pragma unroll
+    for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+      for (int fj = 0; fj < 3; ++fj) l1[fi] += fabsf(vals[(size_t)(s * 9 + fi * 3 + fj) * np + n]);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float dg = vals[(size_t)(13 * 9 + d * 4) * np + n];
+    kinv[(size_t)n * 3 + d] = 1.f / fmaxf(dg / omega, c * l1[d]);
+  }
 }
 
 // t_l = b_l - A_l x_l (zero on boundary nodes).
@@ -399,6 +437,13 @@ int mgb_launch_mg_rap(const MeshDev *mf, const MeshDev *mc, const Inst *insts, c
                       cudaStream_t s) {
   if (nlist <= 0) return 0;
   k_mg_rap<<<dim3(cdiv((size_t)27 * mc->nn, kMgBlock), nlist), kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_sdiag(const MeshDev *m, const Inst *insts, const int *list, int nlist, int l, float omega,
+                        float c, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_mg_sdiag<<<dim3(cdiv(m->nn, kMgBlock), nlist), kMgBlock, 0, s>>>(*m, insts, list, l, omega, c);
   return (int)cudaGetLastError();
 }
 

@@ -58,11 +58,10 @@ constexpr int kSpmvNodes = 4;       // FP32 SpMV: consecutive nodes per thread (
 // by the engine's autotuner.
 constexpr int kSpmv6Nodes = 2;      // 6-RHS SpMV: consecutive nodes per thread (one 8-byte load per entry)
 
-// zscale: 1 for Jacobi-preconditioned CG; the multigrid weight w when a V-cycle follows (z = w D^-1 r is then
-// its pre-smoothed level-0 iterate, and the V-cycle's last kernel sets p and rz).  ||D^-1 r|| stays the norm of
-// the stop test either way.
-__global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list,
-                                                           float zscale) {
+// mg: a V-cycle follows; z is then its pre-smoothed level-0 iterate, the smoother's inverse diagonal (lv[0].kinv)
+// times r, and the V-cycle's last kernel sets p and rz.  ||D^-1 r|| with the plain diagonal stays the norm of the
+// stop test either way.
+__global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst *insts, const int *list, int mg) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   float acc[2] = {0.f, 0.f};
@@ -76,13 +75,14 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_setup(MeshDev m, const Inst
     float *__restrict__ rv = I.r32;
     float *__restrict__ zv = I.z32;
     float *__restrict__ pv = I.p32;
+    const float *__restrict__ ks = mg ? I.mg->lv[0].kinv : nullptr;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int row = n * 3 + d;
       const float kd = b ? 1.0f : 1.0f / vals[ell32_diag(m, n, d)];
       const float r = (float)bb[row];
       const float zj = kd * r;
-      const float z = zscale * zj;
+      const float z = mg ? ks[row] * r : zj;
       kinv[row] = kd;
       du[row] = 0.0f;
       rv[row] = r;
@@ -185,15 +185,14 @@ __global__ void __launch_bounds__(B) k_cg32_spmv(MeshDev m, const Inst *insts, c
 
 // du += alpha p; r -= alpha Ap; z = kinv r, kRowsPerThread rows per thread (loads of all rows first); the
 // last block sets beta, the norms and the stop flag.
-// mg: a V-cycle follows; z = w D^-1 r (its pre-smoothed level-0 iterate) and beta, rz are left to the V-cycle's
-// last kernel.  The stop test uses ||D^-1 r|| in both cases.
-__global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Inst *insts, const int *list, int mg,
-                                                            float omega) {
+// mg: a V-cycle follows; z is its pre-smoothed level-0 iterate (the smoother's inverse diagonal times r) and
+// beta, rz are left to the V-cycle's last kernel.  The stop test uses ||D^-1 r|| in both cases.
+__global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Inst *insts, const int *list, int mg) {
   const Inst &I = insts[list[blockIdx.y]];
   const CgState *cs = I.cg;
   if (cs->done) return;
   const float alpha = (float)cs->alpha;
-  const float zscale = mg ? omega : 1.0f;
+  const float *__restrict__ ks = mg ? I.mg->lv[0].kinv : nullptr;
   const int nrow = m.nn * 3;
   float *__restrict__ du = I.du32;
   float *__restrict__ rv = I.r32;
@@ -219,7 +218,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg32_update(MeshDev m, const Ins
         du[row] = fmaf(alpha, pv[q], dv[q]);
         const float r = fmaf(-alpha, av[q], rr[q]);
         const float zj = kv[q] * r;
-        const float z = zscale * zj;
+        const float z = mg ? ks[row] * r : zj;
         rv[row] = r;
         zv[row] = z;
         acc[0] = fmaf(zj, zj, acc[0]);
@@ -349,9 +348,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *in
 // Refinement residual RF = F - K X (FP64 accumulation), start of a 6-RHS CG on it:
 // R = RF (FP32), D = 0, Z = kinv R, P = Z; the last block initialises the six CG states.  x_zero: X is
 // still 0 (the first sweep), RF = F without the product.
-// zscale as in k_cg32_setup.
+// mg as in k_cg32_setup.
 __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Inst *insts, const int *list,
-                                                            int x_zero, float zscale) {
+                                                            int x_zero, int mg) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[18];
@@ -367,9 +366,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) rf[r][d] = b ? 0.0 : I.F6[c6(r, d, np) + n];
-    float kd[3];
+    float kd[3], ksm[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) kd[d] = I.kinv32[n * 3 + d];
+    for (int d = 0; d < 3; ++d) {
+      kd[d] = I.kinv32[n * 3 + d];
+      ksm[d] = mg ? I.mg->lv[0].kinv[n * 3 + d] : kd[d];
+    }
     if (!b && !x_zero) {
 #pragma unroll 1
       for (int s = 0; s < 27; ++s) {
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
         const size_t idx = c6(r, d, np) + n;
         const float rr = (float)rf[r][d];
         const float zj = kd[d] * rr;
-        const float z = zscale * zj;
+        const float z = ksm[d] * rr;
         R6[idx] = rr;
         Z6[idx] = z;
         P6[idx] = z;
@@ -517,12 +519,10 @@ constexpr int kVec6Chunk = kVec6PerThread * kNodeBlock;
 // chunk through the 18 components in turn (the 16 loads of a component in flight together); an instance has
 // nn / kVec6Chunk blocks to reduce, and the last one sets beta_i and the stop flags.
 // mg as in k_cg32_update.
-__global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list, int mg,
-                                                           float omega) {
+__global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst *insts, const int *list, int mg) {
   const Inst &I = insts[list[blockIdx.y]];
   const Cg6State *cs = I.cg6;
   if (cs->all_done) return;
-  const float zscale = mg ? omega : 1.0f;
   float alpha[6];
   bool live[6];
 #pragma unroll
@@ -535,12 +535,15 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
   for (int q = 0; q < 12; ++q) acc[q] = 0.f;  // [0,6): z.z  [6,12): r.z
   const size_t np = m.np;
   const int n0 = blockIdx.x * kVec6Chunk + threadIdx.x;
-  float kd[kVec6PerThread][3];
+  float kd[kVec6PerThread][3], ksm[kVec6PerThread][3];
 #pragma unroll
   for (int q = 0; q < kVec6PerThread; ++q) {
     const int n = n0 + q * kNodeBlock;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) kd[q][d] = (n < m.nn) ? I.kinv32[n * 3 + d] : 0.f;
+    for (int d = 0; d < 3; ++d) {
+      kd[q][d] = (n < m.nn) ? I.kinv32[n * 3 + d] : 0.f;
+      ksm[q][d] = (n < m.nn && mg) ? I.mg->lv[0].kinv[n * 3 + d] : kd[q][d];
+    }
   }
 #pragma unroll
   for (int r = 0; r < 6; ++r) {
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_update(MeshDev m, const Inst
           D6[n] = fmaf(alpha[r], pv[q], dv[q]);
           const float rr = fmaf(-alpha[r], av[q], rv[q]);
           const float zj = kd[q][d] * rr;
-          const float z = zscale * zj;
+          const float z = ksm[q][d] * rr;
           R6[n] = rr;
           Z6[n] = z;
           acc[r] = fmaf(zj, zj, acc[r]);
@@ -807,10 +810,9 @@ static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) 
 
 extern "C" {
 
-int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, int nlist, float zscale,
-                          cudaStream_t s) {
+int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg32_setup<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, zscale);
+  k_cg32_setup<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg);
   return (int)cudaGetLastError();
 }
 
@@ -827,11 +829,10 @@ int mgb_launch_cg32_spmv(const MeshDev *m, const Inst *insts, const int *list, i
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg32_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, float omega,
-                           cudaStream_t s) {
+int mgb_launch_cg32_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, cudaStream_t s) {
   if (nlist <= 0) return 0;
   const unsigned g = cdiv((size_t)m->nn * 3, (size_t)kRowsPerThread * kNodeBlock);
-  k_cg32_update<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg, omega);
+  k_cg32_update<<<dim3(g, nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg);
   return (int)cudaGetLastError();
 }
 
@@ -862,10 +863,10 @@ int mgb_launch_t6_rhs(const MeshDev *m, const Inst *insts, const int *list, int 
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, int x_zero, float zscale,
+int mgb_launch_t6_residual(const MeshDev *m, const Inst *insts, const int *list, int nlist, int x_zero, int mg,
                            cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, x_zero, zscale);
+  k_t6_residual<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list, x_zero, mg);
   return (int)cudaGetLastError();
 }
 
@@ -881,10 +882,9 @@ int mgb_launch_cg6_spmv(const MeshDev *m, const Inst *insts, const int *list, in
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, float omega,
-                          cudaStream_t s) {
+int mgb_launch_cg6_update(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_cg6_update<<<dim3(cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg, omega);
+  k_cg6_update<<<dim3(cdiv(m->nn, kVec6Chunk), nlist), kNodeBlock, 0, s>>>(*m, insts, list, mg);
   return (int)cudaGetLastError();
 }
 
