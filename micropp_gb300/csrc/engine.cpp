@@ -840,7 +840,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
   }
   launches_ += 1;
   check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, n, mg ? 1 : 0, stream_), "cg32 setup");
-  if (mg) mg_vcycle(1, n, true);
+  if (mg) mg_vcycle(1, n, true, 128);
   const int block = tuned_block(0, n);
   const double nrow = (double)nndim();
   const double spmv_bytes = nrow * (81.0 * 4 + 2.0 * 4);  // per iteration and instance, as in cg_solve
@@ -857,7 +857,7 @@ void Engine::cg_solve32(const std::vector<int> &slots, const std::vector<double>
         timer_begin(t_update_, 0.0);
         check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, n, mg ? 1 : 0, stream_), "cg32 update");
         timer_end(t_update_);
-        if (mg) mg_vcycle(1, n, false);
+        if (mg) mg_vcycle(1, n, false, 128);
         timer_begin(t_update_, 0.0);
         check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, n, d_count_, stream_), "cg32 p-update");
         timer_end(t_update_);
@@ -945,14 +945,16 @@ double Engine::mg_coarse_bytes(int nr) const {
   return b;
 }
 
-// One V-cycle of the nr-RHS CG of the listed instances (their level-0 iterate x0 = w D^-1 r is already
-// written), ending with the level-0 post-smoother that forms z and the CG scalars.
-void Engine::mg_vcycle(int nr, int nlist, bool setup) {
+// One V-cycle of the nr-RHS CG of the listed instances (their level-0 iterate x0 = D^-1 r is already
+// written), ending with the level-0 post-smoother that forms z and the CG scalars.  block: threads per block of
+// the 6-RHS level-0 residual (the tuned block of the 6-RHS SpMV, whose access pattern it shares).
+void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
   const int L = (int)mg_mesh_.size();
   KernelTimer &fine = (nr == 1) ? t_mg1_ : t_mg6_;
   for (int l = 0; l + 1 < L; ++l) {
     if (l == 0) timer_begin(fine, 0.0);
-    check_launch(mgb_launch_mg_resid(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, stream_), "multigrid residual");
+    check_launch(mgb_launch_mg_resid(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, block, stream_),
+                 "multigrid residual");
     if (l == 0) {
       timer_end(fine);
       timer_begin(t_mgc_, 0.0);
@@ -1047,8 +1049,8 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
                    "tangent residual");
     }
     const int nl = (int)live.size();
-    if (mg) mg_vcycle(6, nl, true);
     const int block = tuned_block(1, nl);
+    if (mg) mg_vcycle(6, nl, true, block);
     int done_its = 0;
     while (done_its <= cg_max_its_) {
       run_chunk(mg ? 2 : 4, nl, [&] {
@@ -1060,7 +1062,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
           timer_begin(t_upd6_, 0.0);
           check_launch(mgb_launch_cg6_update(&mesh_, d_insts_, d_list_, nl, mg ? 1 : 0, stream_), "cg6 update");
           timer_end(t_upd6_);
-          if (mg) mg_vcycle(6, nl, false);
+          if (mg) mg_vcycle(6, nl, false, block);
           timer_begin(t_upd6_, 0.0);
           check_launch(mgb_launch_cg6_pupdate(&mesh_, d_insts_, d_list_, nl, d_count_, stream_), "cg6 p-update");
           timer_end(t_upd6_);

@@ -81,8 +81,9 @@ int mgb_launch_mg_rap(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb:
 // Inverse safeguarded smoother diagonal of level l: 1 / max(a_dd / omega, c sum_j |a_dj|).
 int mgb_launch_mg_sdiag(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int l,
                         float omega, float c, cudaStream_t s);
+// block: threads per block of the 6-RHS level-0 residual (64, 128 or 256; two nodes per thread).
 int mgb_launch_mg_resid(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
-                        cudaStream_t s);
+                        int block, cudaStream_t s);
 int mgb_launch_mg_restrict(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,
                            int nlist, int nr, int lf, float omega, cudaStream_t s);
 int mgb_launch_mg_prolong(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,

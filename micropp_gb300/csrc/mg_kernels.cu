@@ -366,6 +366,34 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_jacobi(MeshDev m, const Inst *i
     }
 }
 
+// The CG scalars after the level-0 post-smoother (last block of the instance, thread 0): setup sets rz, an
+// iteration beta and rz, for the right-hand sides still iterating.
+template <int NR>
+__device__ __forceinline__ void post0_scalars(const Inst &I, const double (&tot)[NR], int setup) {
+  if (NR == 1) {
+    CgState *c = I.cg;
+    if (!setup) c->beta = tot[0] / c->rz;
+    c->rz = tot[0];
+    if (!isfinite(tot[0])) {
+      c->done = 1;
+      I.out->nonfinite = 1;
+      I.out->cg_its = c->its;
+    }
+  } else {
+    Cg6State *c = I.cg6;
+    for (int r = 0; r < NR; ++r) {
+      if (c->done[r]) continue;
+      if (!setup) c->beta[r] = tot[r] / c->rz[r];
+      c->rz[r] = tot[r];
+      if (!isfinite(tot[r])) c->done[r] = 1;
+    }
+    int all = 1;
+    for (int r = 0; r < NR; ++r) all &= c->done[r];
+    c->all_done = all;
+    if (all) I.out->cg6_its = c->its;
+  }
+}
+
 // Level-0 post-smoother and the CG scalars: z = t0 + w D^-1 (r - A t0), rz_i = sum r.z.  setup: p = z and
 // rz = rz_i (start of a solve); otherwise beta = rz_i / rz, rz = rz_i (right-hand sides still iterating).
 template <int NR, bool RM>
@@ -398,28 +426,78 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_post0(MeshDev m, const Inst *in
       }
   }
   double tot[NR];
-  if (grid_sum_f<NR>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
-    if (NR == 1) {
-      CgState *c = I.cg;
-      if (!setup) c->beta = tot[0] / c->rz;
-      c->rz = tot[0];
-      if (!isfinite(tot[0])) {
-        c->done = 1;
-        I.out->nonfinite = 1;
-        I.out->cg_its = c->its;
-      }
-    } else {
-      Cg6State *c = I.cg6;
-      for (int r = 0; r < NR; ++r) {
-        if (c->done[r]) continue;
-        if (!setup) c->beta[r] = tot[r] / c->rz[r];
-        c->rz[r] = tot[r];
-        if (!isfinite(tot[r])) c->done[r] = 1;
-      }
-      int all = 1;
-      for (int r = 0; r < NR; ++r) all &= c->done[r];
-      c->all_done = all;
-      if (all) I.out->cg6_its = c->its;
+  if (grid_sum_f<NR>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) post0_scalars<NR>(I, tot, setup);
+}
+
+// Level-0 residual of the 6-RHS V-cycle with the structure of the tangent CG's SpMV: two consecutive nodes per
+// thread (n0 even; np is a multiple of 32, so each ELL entry of the pair is one 8-byte load), the 4 neighbours
+// of a pair row along x loaded once for the 3 x-slots, neighbour indices clamped into the grid (the sums of
+// boundary nodes are discarded).  Same products and order per row as apply_node.  Held to 128 registers (512
+// threads per SM), the residency of the tangent CG's SpMV.
+__device__ __forceinline__ void apply_pair6(const MeshDev &m, const float *__restrict__ vals,
+                                            const float *__restrict__ x, int n0, float (&y)[2][18]) {
+  const size_t np = m.np, np2 = np / 2;
+  const float2 *__restrict__ v2 = reinterpret_cast<const float2 *>(vals + n0);
+  const int last = m.nn - 1;
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < 18; ++c) y[q][c] = 0.f;
+#pragma unroll 1
+  for (int zy = 0; zy < 9; ++zy) {
+    const int base = n0 + (zy / 3 - 1) * m.nxny + (zy % 3 - 1) * m.nx - 1;
+    int nb[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) nb[w] = min(max(base + w, 0), last);
+    float2 a[3][9];
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) a[dx][e] = __ldcs(v2 + (size_t)((zy * 3 + dx) * 9 + e) * np2);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      float xv[4][3];
+#pragma unroll
+      for (int w = 0; w < 4; ++w)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) xv[w][d] = x[(size_t)(r * 3 + d) * np + nb[w]];
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+          const int fi = e / 3, fj = e % 3;
+          y[0][r * 3 + fi] = fmaf(a[dx][e].x, xv[dx][fj], y[0][r * 3 + fi]);
+          y[1][r * 3 + fi] = fmaf(a[dx][e].y, xv[1 + dx][fj], y[1][r * 3 + fi]);
+        }
+    }
+  }
+}
+
+// t0 = r - A x0 for the 6 right-hand sides (zero on boundary nodes), two nodes per thread.
+template <int B>
+__global__ void __launch_bounds__(B, 512 / B) k_mg_resid6(MeshDev m, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (I.cg6->all_done) return;
+  const int n0 = (blockIdx.x * B + threadIdx.x) * 2;
+  if (n0 >= m.nn) return;
+  const LvView v = view<6>(I, 0);
+  const size_t np = m.np;
+  bool bn[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    int i, j, k;
+    bn[q] = (n0 + q >= m.nn) || on_boundary(m, n0 + q, i, j, k);
+  }
+  float y[2][18];
+  if (!bn[0] || !bn[1]) apply_pair6(m, v.vals, v.x, n0, y);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int n = n0 + q;
+    if (n >= m.nn) break;
+#pragma unroll
+    for (int c = 0; c < 18; ++c) {
+      const size_t idx = (size_t)c * np + n;
+      v.t[idx] = bn[q] ? 0.f : v.b[idx] - y[q][c];
     }
   }
 }
@@ -447,9 +525,19 @@ int mgb_launch_mg_sdiag(const MeshDev *m, const Inst *insts, const int *list, in
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_mg_resid(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l,
+int mgb_launch_mg_resid(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l, int block,
                         cudaStream_t s) {
   if (nlist <= 0) return 0;
+  if (nr == 6 && l == 0) {
+    const size_t pairs = cdiv(m->nn, 2);
+    if (block == 64)
+      k_mg_resid6<64><<<dim3(cdiv(pairs, 64), nlist), 64, 0, s>>>(*m, insts, list);
+    else if (block == 256)
+      k_mg_resid6<256><<<dim3(cdiv(pairs, 256), nlist), 256, 0, s>>>(*m, insts, list);
+    else
+      k_mg_resid6<128><<<dim3(cdiv(pairs, 128), nlist), 128, 0, s>>>(*m, insts, list);
+    return (int)cudaGetLastError();
+  }
   const dim3 g(cdiv(m->nn, kMgBlock), nlist);
   if (nr == 1) {
     if (l == 0)
@@ -457,10 +545,7 @@ int mgb_launch_mg_resid(const MeshDev *m, const Inst *insts, const int *list, in
     else
       k_mg_resid<1, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
   } else {
-    if (l == 0)
-      k_mg_resid<6, false, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
-    else
-      k_mg_resid<6, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+    k_mg_resid<6, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
   }
   return (int)cudaGetLastError();
 }
