@@ -100,6 +100,7 @@ struct MgLevel {
 
 struct MgInst {
   MgLevel lv[kMgMaxLevels];
+  float *mid1, *mid2;      // the separable Galerkin product's intermediate operators (x, then x and y coarsened)
 };
 
 struct Inst {

@@ -48,6 +48,22 @@ constexpr int kMgCoarsePairs = 4;
 constexpr int kMgChunk = 4;
 constexpr int kMgMaxIts = 100;
 
+// A structured grid of nx x ny x nz nodes (the multigrid levels and the separable product's intermediates).
+static MeshDev grid_of(int nx, int ny, int nz) {
+  MeshDev g{};
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.nex = nx - 1;
+  g.ney = ny - 1;
+  g.nez = nz - 1;
+  g.nelem = g.nex * g.ney * g.nez;
+  g.nxny = nx * ny;
+  g.nn = g.nxny * nz;
+  g.np = (g.nn + 31) / 32 * 32;
+  return g;
+}
+
 const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
 }  // namespace
@@ -110,18 +126,7 @@ Engine::Engine(const micropp3_config &cfg) {
       const int lo = std::min(ne[0], std::min(ne[1], ne[2])), hi = std::max(ne[0], std::max(ne[1], ne[2]));
       if (lo < 4 || hi <= 4) break;
       for (int &e : ne) e = (e + 1) / 2;
-      MeshDev c{};
-      c.nex = ne[0];
-      c.ney = ne[1];
-      c.nez = ne[2];
-      c.nelem = ne[0] * ne[1] * ne[2];
-      c.nx = ne[0] + 1;
-      c.ny = ne[1] + 1;
-      c.nz = ne[2] + 1;
-      c.nxny = c.nx * c.ny;
-      c.nn = c.nxny * c.nz;
-      c.np = (c.nn + 31) / 32 * 32;
-      mg_mesh_.push_back(c);
+      mg_mesh_.push_back(grid_of(ne[0] + 1, ne[1] + 1, ne[2] + 1));
     }
     mg_ = pc == MICROPP3_PRECOND_MG && mg_mesh_.size() >= 2;
     if (pc == MICROPP3_PRECOND_MG && !mg_)
@@ -448,6 +453,8 @@ double Engine::slot_bytes() const {
   if (mg_) {
     b += 4.0 * 21.0 * np;
     for (size_t l = 1; l < mg_mesh_.size(); ++l) b += 4.0 * (kEllPerNode + 3.0 + 4.0 * 18.0) * mg_mesh_[l].np;
+    const MeshDev &c = mg_mesh_[1];
+    b += 4.0 * kEllPerNode * (grid_of(c.nx, mesh_.ny, mesh_.nz).np + grid_of(c.nx, c.ny, mesh_.nz).np);
   }
   return b;
 }
@@ -515,6 +522,11 @@ void Engine::ensure_slots(int n) {
       };
       h.lv[0].t = buf((size_t)18 * mesh_.np, "multigrid level-0 residual");
       h.lv[0].kinv = buf((size_t)3 * mesh_.np, "multigrid level-0 smoother diagonal");
+      {
+        const MeshDev &c = mg_mesh_[1];  // the first product has the largest intermediates
+        h.mid1 = buf((size_t)kEllPerNode * grid_of(c.nx, mesh_.ny, mesh_.nz).np, "multigrid intermediate operator");
+        h.mid2 = buf((size_t)kEllPerNode * grid_of(c.nx, c.ny, mesh_.nz).np, "multigrid intermediate operator");
+      }
       for (size_t l = 1; l < mg_mesh_.size(); ++l) {
         const size_t np = mg_mesh_[l].np;
         h.lv[l].vals = buf((size_t)kEllPerNode * np, "multigrid operator");
@@ -899,25 +911,33 @@ void Engine::assemble32(int nlist) {
   if (mg_) mg_rap(nlist);
 }
 
-// Galerkin operators P^T A P of every coarse level, finest first, and the safeguarded smoother diagonal of
-// every level.  Algorithmic bytes: each level's operator read twice (product, diagonal) and the next one written
-// once.
+// Galerkin operators P^T A P of every coarse level, finest first, each as three 1-D steps (x, y, z) through
+// the intermediate operators mid1 and mid2, and the safeguarded smoother diagonal of every level.  Algorithmic
+// bytes: each step reads its input operator and writes its output once; each level's diagonal reads its operator.
 void Engine::mg_rap(int nlist) {
   double bytes = 0.0;
   for (size_t l = 0; l < mg_mesh_.size(); ++l) {
-    bytes += 4.0 * kEllPerNode * (double)mg_mesh_[l].np;
-    if (l + 1 < mg_mesh_.size()) bytes += 4.0 * kEllPerNode * (double)(mg_mesh_[l].np + mg_mesh_[l + 1].np);
+    const MeshDev &f = mg_mesh_[l];
+    bytes += 4.0 * kEllPerNode * (double)f.np;
+    if (l + 1 < mg_mesh_.size()) {
+      const MeshDev &c = mg_mesh_[l + 1];
+      const double n1 = grid_of(c.nx, f.ny, f.nz).np, n2 = grid_of(c.nx, c.ny, f.nz).np;
+      bytes += 4.0 * kEllPerNode * ((double)f.np + 2.0 * n1 + 2.0 * n2 + (double)c.np);
+    }
   }
   timer_begin(t_asm_, nlist * bytes);
   launches_ += 1;
   check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
                "multigrid smoother diagonal");
   for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l) {
-    launches_ += 2;
-    check_launch(mgb_launch_mg_rap(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, (int)l, stream_),
-                 "multigrid Galerkin operator");
-    check_launch(mgb_launch_mg_sdiag(&mg_mesh_[l + 1], d_insts_, d_list_, nlist, (int)l + 1, kMgOmega, kMgSafe,
-                                     stream_),
+    const MeshDev &f = mg_mesh_[l], &c = mg_mesh_[l + 1];
+    const MeshDev m1 = grid_of(c.nx, f.ny, f.nz), m2 = grid_of(c.nx, c.ny, f.nz);
+    const int lf = (int)l;
+    launches_ += 4;
+    check_launch(mgb_launch_mg_rap1(&f, &m1, d_insts_, d_list_, nlist, lf, 0, 0, 1, stream_), "multigrid product x");
+    check_launch(mgb_launch_mg_rap1(&m1, &m2, d_insts_, d_list_, nlist, lf, 1, 1, 2, stream_), "multigrid product y");
+    check_launch(mgb_launch_mg_rap1(&m2, &c, d_insts_, d_list_, nlist, lf, 2, 2, 3, stream_), "multigrid product z");
+    check_launch(mgb_launch_mg_sdiag(&c, d_insts_, d_list_, nlist, lf + 1, kMgOmega, kMgSafe, stream_),
                  "multigrid smoother diagonal");
   }
   timer_end(t_asm_);

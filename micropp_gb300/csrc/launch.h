@@ -76,8 +76,10 @@ int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8
 // Geometric multigrid preconditioner of the mixed form's FP32 CG (mg_kernels.cu).  mf / mc: the grids of levels
 // lf and lf + 1; nr: 1 (the Newton CG's vectors) or 6 (the tangent CG's).  src / dst of the Jacobi sweep:
 // 0 = x, 1 = y, 2 = t of level l >= 1.
-int mgb_launch_mg_rap(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,
-                      int nlist, int lf, cudaStream_t s);
+// One 1-D step of the separable Galerkin product (axis 0, 1, 2): operator on grid mi -> grid mo.  src / dst:
+// 0 = level lf's operator, 1 / 2 = the intermediate operators, 3 = level lf + 1's operator.
+int mgb_launch_mg_rap1(const mgb::MeshDev *mi, const mgb::MeshDev *mo, const mgb::Inst *insts, const int *list,
+                       int nlist, int lf, int axis, int src, int dst, cudaStream_t s);
 // Inverse safeguarded smoother diagonal of level l: 1 / max(a_dd / omega, c sum_j |a_dj|).
 int mgb_launch_mg_sdiag(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int l,
                         float omega, float c, cudaStream_t s);

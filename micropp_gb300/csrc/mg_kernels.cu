@@ -7,7 +7,8 @@
 // coarse parent with weight 1, an odd one its two neighbours with weight 1/2.  Corrections vanish on boundary
 // nodes (Dirichlet rows), so P only couples interior nodes.  The coarse operator is the Galerkin product
 // A_c = P^T A P; with trilinear P and a 27-point operator it is again a 27-point operator of 3x3 blocks, so
-// every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].
+// every level uses the fine level's stencil ELL layout, vals[(s * 9 + fi * 3 + fj) * np + n].  P is a tensor
+// product of 1-D interpolations, so the product is formed one axis at a time (k_mg_rap1).
 //
 // The preconditioner is one V-cycle with a damped-Jacobi smoother before and after the coarse correction and a
 // fixed number of Jacobi sweeps on the coarsest level.  The smoother's diagonal is safeguarded per row:
@@ -118,71 +119,64 @@ __device__ __forceinline__ void apply_node(const MeshDev &m, const float *__rest
   }
 }
 
-// Galerkin coarse operator of level lf + 1 from level lf: thread (S, I) forms the 3x3 block of coarse node I
-// toward coarse neighbour J = I + offset(S):
-//   A_c[I][S] = sum_{a, o} P[i][I] A[i][o] P[j][J],  i = 2I + a, j = i + o,  a, o in {-1, 0, 1}^3,
-// over fine interior i and j; P[i][I] = prod_d 2^-|a_d|, P[j][J] = prod_d 2^-|j_d - 2 J_d| (zero beyond 1).
-// Coarse boundary rows become identity rows; blocks toward coarse boundary nodes are zero.  The order of the
-// additions is fixed.
-__global__ void __launch_bounds__(kMgBlock) k_mg_rap(MeshDev mf, MeshDev mc, const Inst *insts, const int *list,
-                                                     int lf) {
+// One 1-D step of the separable Galerkin product: P = Px Py Pz (each a 1-D interpolation with the Dirichlet
+// rows and columns of its axis removed), so P^T A P = Pz^T (Py^T (Px^T A Px) Py) Pz.  The step along `axis` maps
+// the operator on grid mi to the operator on grid mo, mi with that axis coarsened to ceil(n / 2) elements; the
+// other axes pass through.  Thread (S, io) forms the 3x3 block of output node io toward its neighbour at offset
+// S from at most 7 input blocks:
+//   B[io][S] = sum_{a, o} 2^-|a| 2^-|e| A[i][s'],  i = io with 2X + a on the axis, j = i + o on the axis,
+//   e = j - 2 (X + S_axis), s' = S with o on the axis,
+// over i and j interior along the axis.  Rows and columns on the axis' boundary are zero; in the last step
+// (dst = 3, the next level's operator) boundary rows become identity rows.  The order of the additions is
+// fixed.  src / dst: 0 = level lf's operator, 1 = mid1, 2 = mid2, 3 = level lf + 1's operator.
+__global__ void __launch_bounds__(kMgBlock) k_mg_rap1(MeshDev mi, MeshDev mo, const Inst *insts, const int *list,
+                                                      int lf, int axis, int src, int dst) {
   const Inst &I = insts[list[blockIdx.y]];
-  const float *__restrict__ Af = (lf == 0) ? I.vals32 : I.mg->lv[lf].vals;
-  const MgLevel &C = I.mg->lv[lf + 1];
+  const MgInst &G = *I.mg;
+  const float *__restrict__ A = src == 0 ? (lf == 0 ? I.vals32 : G.lv[lf].vals) : src == 1 ? G.mid1 : G.mid2;
+  float *__restrict__ B = dst == 3 ? G.lv[lf + 1].vals : dst == 1 ? G.mid1 : G.mid2;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 27 * mc.nn) return;
-  const int S = t / mc.nn, ic = t - S * mc.nn;
-  int X, Y, Z;
-  const bool cb = on_boundary(mc, ic, X, Y, Z);
-  const int SX = S % 3 - 1, SY = (S / 3) % 3 - 1, SZ = S / 9 - 1;
-  const int JX = X + SX, JY = Y + SY, JZ = Z + SZ;
-  const bool jb = JX <= 0 || JY <= 0 || JZ <= 0 || JX >= mc.nx - 1 || JY >= mc.ny - 1 || JZ >= mc.nz - 1;
+  if (t >= 27 * mo.nn) return;
+  const int S = t / mo.nn, io = t - S * mo.nn;
+  int c[3] = {io % mo.nx, (io / mo.nx) % mo.ny, io / mo.nxny};
+  const int so[3] = {S % 3 - 1, (S / 3) % 3 - 1, S / 9 - 1};
+  const int dimo[3] = {mo.nx, mo.ny, mo.nz}, dimi[3] = {mi.nx, mi.ny, mi.nz};
+  const int X = c[axis], JX = X + so[axis];
+  bool live = X > 0 && X < dimo[axis] - 1 && JX > 0 && JX < dimo[axis] - 1;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (d != axis && (c[d] + so[d] < 0 || c[d] + so[d] > dimo[d] - 1)) live = false;
   float acc[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = 0.f;
-  if (!cb && !jb) {
-    const size_t npf = mf.np;
-#pragma unroll 1
-    for (int az = -1; az <= 1; ++az) {
-      const int iz = 2 * Z + az;
-      if (iz <= 0 || iz >= mf.nz - 1) continue;
-#pragma unroll 1
-      for (int ay = -1; ay <= 1; ++ay) {
-        const int iy = 2 * Y + ay;
-        if (iy <= 0 || iy >= mf.ny - 1) continue;
-#pragma unroll 1
-        for (int ax = -1; ax <= 1; ++ax) {
-          const int ix = 2 * X + ax;
-          if (ix <= 0 || ix >= mf.nx - 1) continue;
-          const float wi = half_pow(ax) * half_pow(ay) * half_pow(az);
-          const int i = (iz * mf.ny + iy) * mf.nx + ix;
-#pragma unroll 1
-          for (int oz = -1; oz <= 1; ++oz) {
-            const int jz = iz + oz, ez = jz - 2 * JZ;
-            if (ez < -1 || ez > 1 || jz <= 0 || jz >= mf.nz - 1) continue;
-#pragma unroll 1
-            for (int oy = -1; oy <= 1; ++oy) {
-              const int jy = iy + oy, ey = jy - 2 * JY;
-              if (ey < -1 || ey > 1 || jy <= 0 || jy >= mf.ny - 1) continue;
+  if (live) {
+    const size_t npi = mi.np;
 #pragma unroll
-              for (int ox = -1; ox <= 1; ++ox) {
-                const int jx = ix + ox, ex = jx - 2 * JX;
-                if (ex < -1 || ex > 1 || jx <= 0 || jx >= mf.nx - 1) continue;
-                const float w = wi * half_pow(ex) * half_pow(ey) * half_pow(ez);
-                const int sf = (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1);
+    for (int a = -1; a <= 1; ++a) {
+      const int ix = 2 * X + a;
+      if (ix <= 0 || ix >= dimi[axis] - 1) continue;
+      int f[3] = {c[0], c[1], c[2]};
+      f[axis] = ix;
+      const int i = f[0] + mi.nx * (f[1] + mi.ny * f[2]);
 #pragma unroll
-                for (int q = 0; q < 9; ++q) acc[q] = fmaf(w, __ldg(Af + (size_t)(sf * 9 + q) * npf + i), acc[q]);
-              }
-            }
-          }
-        }
+      for (int o = -1; o <= 1; ++o) {
+        const int jx = ix + o, e = jx - 2 * JX;
+        if (e < -1 || e > 1 || jx <= 0 || jx >= dimi[axis] - 1) continue;
+        int off[3] = {so[0], so[1], so[2]};
+        off[axis] = o;
+        const int sf = (off[2] + 1) * 9 + (off[1] + 1) * 3 + (off[0] + 1);
+        const float w = half_pow(a) * half_pow(e);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] = fmaf(w, __ldg(A + (size_t)(sf * 9 + q) * npi + i), acc[q]);
       }
     }
-  } else if (cb && S == 13) {
-    acc[0] = acc[4] = acc[8] = 1.f;
+  }
+  if (dst == 3 && S == 13) {
+    int i, j, k;
+    if (on_boundary(mo, io, i, j, k)) acc[0] = acc[4] = acc[8] = 1.f;
   }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) C.vals[(size_t)(S * 9 + q) * mc.np + ic] = acc[q];
+  for (int q = 0; q < 9; ++q) B[(size_t)(S * 9 + q) * mo.np + io] = acc[q];
 }
 
 // Inverse of the safeguarded smoother diagonal of level l, per row (n, d):
@@ -511,10 +505,12 @@ using namespace mgb;
 
 extern "C" {
 
-int mgb_launch_mg_rap(const MeshDev *mf, const MeshDev *mc, const Inst *insts, const int *list, int nlist, int lf,
-                      cudaStream_t s) {
+int mgb_launch_mg_rap1(const MeshDev *mi, const MeshDev *mo, const Inst *insts, const int *list, int nlist, int lf,
+                       int axis, int src, int dst, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_mg_rap<<<dim3(cdiv((size_t)27 * mc->nn, kMgBlock), nlist), kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
+  if (axis < 0 || axis > 2 || src < 0 || src > 2 || dst < 1 || dst > 3 || src == dst) return (int)cudaErrorInvalidValue;
+  k_mg_rap1<<<dim3(cdiv((size_t)27 * mo->nn, kMgBlock), nlist), kMgBlock, 0, s>>>(*mi, *mo, insts, list, lf, axis, src,
+                                                                               dst);
   return (int)cudaGetLastError();
 }
 
