@@ -785,7 +785,8 @@ void Engine::residual(const std::vector<int> &slots) {
   const double bytes = (double)slots.size() * (16.0 * nndim() + 8.0 * nvars());
   timer_begin(t_res_, bytes);
   launches_ += 2;
-  check_launch(mgb_launch_residual(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, (int)slots.size(), stream_),
+  check_launch(mgb_launch_residual(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, (int)slots.size(),
+                                   precision_ == MICROPP3_FP64 ? 1 : 0, stream_),
                "residual");
   timer_end(t_res_);
 }

@@ -98,7 +98,10 @@ __global__ void k_copy(int n, const double *const *src, double *const *dst, cons
 // ---------------------------------------------------------------------------------------------------
 // Element residual blocks be = sum_gp B^T sigma(B u_e, vars) wg (assembly.cpp:123-138), one thread per
 // element, plus the element's share of the volume average of sigma (average.cpp:57-82), reduced over the
-// grid into out.sig.
+// grid into out.sig.  REF: each term formed as (g sigma) wg, the reference's order (the FP64 form, whose
+// iteration counts match the reference's); otherwise sigma wg is formed once per Gauss point and each term is
+// one fused multiply-add (the mixed form: a quarter fewer FP64 operations, rounding within 1e-16 relative).
+template <bool REF>
 __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, const int8_t *etype,
                                                            const double *dsh_g, const Inst *insts,
                                                            const int *list) {
@@ -145,18 +148,31 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, c
       } else {
         law_stress(mat, eps, vg, s);
       }
+      if (REF) {
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
-        be[a * 3 + 0] += gx * s[0] * wg;
-        be[a * 3 + 0] += gy * s[3] * wg;
-        be[a * 3 + 0] += gz * s[4] * wg;
-        be[a * 3 + 1] += gy * s[1] * wg;
-        be[a * 3 + 1] += gx * s[3] * wg;
-        be[a * 3 + 1] += gz * s[5] * wg;
-        be[a * 3 + 2] += gz * s[2] * wg;
-        be[a * 3 + 2] += gx * s[4] * wg;
-        be[a * 3 + 2] += gy * s[5] * wg;
+        for (int a = 0; a < 8; ++a) {
+          const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+          be[a * 3 + 0] += gx * s[0] * wg;
+          be[a * 3 + 0] += gy * s[3] * wg;
+          be[a * 3 + 0] += gz * s[4] * wg;
+          be[a * 3 + 1] += gy * s[1] * wg;
+          be[a * 3 + 1] += gx * s[3] * wg;
+          be[a * 3 + 1] += gz * s[5] * wg;
+          be[a * 3 + 2] += gz * s[2] * wg;
+          be[a * 3 + 2] += gx * s[4] * wg;
+          be[a * 3 + 2] += gy * s[5] * wg;
+        }
+      } else {
+        double sw[6];
+#pragma unroll
+        for (int v = 0; v < 6; ++v) sw[v] = s[v] * wg;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+          be[a * 3 + 0] = fma(gz, sw[4], fma(gy, sw[3], fma(gx, sw[0], be[a * 3 + 0])));
+          be[a * 3 + 1] = fma(gz, sw[5], fma(gx, sw[3], fma(gy, sw[1], be[a * 3 + 1])));
+          be[a * 3 + 2] = fma(gy, sw[5], fma(gx, sw[4], fma(gz, sw[2], be[a * 3 + 2])));
+        }
       }
 #pragma unroll
       for (int v = 0; v < 6; ++v) aux[v] += s[v] * wg;
@@ -640,9 +656,13 @@ int mgb_launch_copy(int n, const double *const *src, double *const *dst, const i
 }
 
 int mgb_launch_residual(const MeshDev *m, const Mats *mats, const int8_t *etype, const double *dsh,
-                        const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+                        const Inst *insts, const int *list, int nlist, int ref_order, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_elem_rhs<<<dim3(cdiv(m->nelem, kElemBlock), nlist), kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
+  const dim3 g(cdiv(m->nelem, kElemBlock), nlist);
+  if (ref_order)
+    k_elem_rhs<true><<<g, kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
+  else
+    k_elem_rhs<false><<<g, kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
   k_node_rhs<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
