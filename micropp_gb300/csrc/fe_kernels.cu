@@ -8,6 +8,7 @@
 #include "device.cuh"
 #include "launch.h"
 #include "adjoint_laws.h"
+#include "hex_sumfact.h"
 #include "laws.cuh"
 #include "reduce.cuh"
 
@@ -98,10 +99,8 @@ __global__ void k_copy(int n, const double *const *src, double *const *dst, cons
 // ---------------------------------------------------------------------------------------------------
 // Element residual blocks be = sum_gp B^T sigma(B u_e, vars) wg (assembly.cpp:123-138), one thread per
 // element, plus the element's share of the volume average of sigma (average.cpp:57-82), reduced over the
-// grid into out.sig.  REF: each term formed as (g sigma) wg, the reference's order (the FP64 form, whose
-// iteration counts match the reference's); otherwise sigma wg is formed once per Gauss point and each term is
-// one fused multiply-add (the mixed form: a quarter fewer FP64 operations, rounding within 1e-16 relative).
-template <bool REF>
+// grid into out.sig.  Each term is formed as (g sigma) wg, the reference's order: the FP64 form's iteration
+// counts match the reference's.  The mixed form uses k_elem_rhs_sf.
 __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, const int8_t *etype,
                                                            const double *dsh_g, const Inst *insts,
                                                            const int *list) {
@@ -148,31 +147,18 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, c
       } else {
         law_stress(mat, eps, vg, s);
       }
-      if (REF) {
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
-          be[a * 3 + 0] += gx * s[0] * wg;
-          be[a * 3 + 0] += gy * s[3] * wg;
-          be[a * 3 + 0] += gz * s[4] * wg;
-          be[a * 3 + 1] += gy * s[1] * wg;
-          be[a * 3 + 1] += gx * s[3] * wg;
-          be[a * 3 + 1] += gz * s[5] * wg;
-          be[a * 3 + 2] += gz * s[2] * wg;
-          be[a * 3 + 2] += gx * s[4] * wg;
-          be[a * 3 + 2] += gy * s[5] * wg;
-        }
-      } else {
-        double sw[6];
-#pragma unroll
-        for (int v = 0; v < 6; ++v) sw[v] = s[v] * wg;
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
-          be[a * 3 + 0] = fma(gz, sw[4], fma(gy, sw[3], fma(gx, sw[0], be[a * 3 + 0])));
-          be[a * 3 + 1] = fma(gz, sw[5], fma(gx, sw[3], fma(gy, sw[1], be[a * 3 + 1])));
-          be[a * 3 + 2] = fma(gy, sw[5], fma(gx, sw[4], fma(gz, sw[2], be[a * 3 + 2])));
-        }
+      for (int a = 0; a < 8; ++a) {
+        const double gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+        be[a * 3 + 0] += gx * s[0] * wg;
+        be[a * 3 + 0] += gy * s[3] * wg;
+        be[a * 3 + 0] += gz * s[4] * wg;
+        be[a * 3 + 1] += gy * s[1] * wg;
+        be[a * 3 + 1] += gx * s[3] * wg;
+        be[a * 3 + 1] += gz * s[5] * wg;
+        be[a * 3 + 2] += gz * s[2] * wg;
+        be[a * 3 + 2] += gx * s[4] * wg;
+        be[a * 3 + 2] += gy * s[5] * wg;
       }
 #pragma unroll
       for (int v = 0; v < 6; ++v) aux[v] += s[v] * wg;
@@ -184,6 +170,87 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, c
   double tot[6];
   const int nb = gridDim.x;
   if (grid_sum<6>(aux, I.red, I.ticket, nb, tot) && threadIdx.x == 0) {
+    bool bad = false;
+#pragma unroll
+    for (int v = 0; v < 6; ++v) {
+      I.out->sig[v] = tot[v] / m.vol_tot;
+      bad |= !isfinite(tot[v]);
+    }
+    if (bad) I.out->nonfinite = 1;
+  }
+}
+
+// The mixed form's element residual by sum factorisation (hex_sumfact.h): the element's 36 nodal differences
+// give the strain at every Gauss point by bilinear interpolation, and the stresses times wg are summed per
+// pair of points before the bilinear weights of the transpose.  About 900 FP64 operations per element against
+// about 2,100 for the B-matrix products, with the same laws, tangent terms and average stress as k_elem_rhs;
+// the rounding differs from the B-matrix order (the FP64 form keeps that order).  The Gauss-point loop is
+// unrolled so each point's accumulator slots are fixed at compile time.
+__global__ void __launch_bounds__(kElemBlock) k_elem_rhs_sf(MeshDev m, Mats mats, const int8_t *etype,
+                                                            const Inst *insts, const int *list) {
+  constexpr double kXg = 0.577350269189626;  // Gauss coordinate (params.hpp:34)
+  const Inst &I = insts[list[blockIdx.y]];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double aux[6] = {0, 0, 0, 0, 0, 0};
+  if (e < m.nelem) {
+    const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
+    const int n0 = ez * m.nxny + ey * m.nx + ex;
+    double D[3][3][4];
+    {
+      double ue[24];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ue[a * 3 + d] = I.u[n * 3 + d];
+      }
+      sf::diffs(ue, D);
+    }
+    const MatDev &mat = mats.m[etype[e]];
+    const double inv4h[3] = {0.25 / m.dx, 0.25 / m.dy, 0.25 / m.dz};
+    const double wg = m.wg;
+    double S[3][3][4];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) S[d][c][k] = 0.0;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      const int gs[3] = {(g == 1 || g == 2 || g == 5 || g == 6) ? 1 : -1, (g == 2 || g == 3 || g == 6 || g == 7) ? 1 : -1,
+                         g >= 4 ? 1 : -1};
+      double gr[3][3], eps[6], sg[6];
+      sf::grad_at(D, gs, kXg, inv4h, gr);
+      sf::strain_of(gr, eps);
+      const double *vg = I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr;
+      if (mat.type == 2 && I.gpd) {
+        double Dm, ta, tc;
+        law_damage_terms(mat, eps, vg, sg, &Dm, &ta, &tc);
+        float *__restrict__ gpd = I.gpd;
+        const size_t st = (size_t)8 * m.nelem, o = (size_t)g * m.nelem + e;
+        gpd[o] = (float)ta;
+        gpd[st + o] = (float)tc;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) gpd[(2 + v) * st + o] = (float)sg[v];
+        const double f = 1 - Dm;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) sg[v] *= f;
+      } else {
+        law_stress(mat, eps, vg, sg);
+      }
+      sf::accumulate(S, gs, sg, wg);
+#pragma unroll
+      for (int v = 0; v < 6; ++v) aux[v] += sg[v] * wg;
+    }
+    double be[24];
+    sf::finish(S, kXg, inv4h, be);
+    double *__restrict__ bev = I.be;
+#pragma unroll
+    for (int i = 0; i < 24; ++i) bev[(size_t)i * m.nelem + e] = be[i];
+  }
+  double tot[6];
+  if (grid_sum<6>(aux, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     bool bad = false;
 #pragma unroll
     for (int v = 0; v < 6; ++v) {
@@ -660,9 +727,9 @@ int mgb_launch_residual(const MeshDev *m, const Mats *mats, const int8_t *etype,
   if (nlist <= 0) return 0;
   const dim3 g(cdiv(m->nelem, kElemBlock), nlist);
   if (ref_order)
-    k_elem_rhs<true><<<g, kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
+    k_elem_rhs<<<g, kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
   else
-    k_elem_rhs<false><<<g, kElemBlock, 0, s>>>(*m, *mats, etype, dsh, insts, list);
+    k_elem_rhs_sf<<<g, kElemBlock, 0, s>>>(*m, *mats, etype, insts, list);
   k_node_rhs<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }

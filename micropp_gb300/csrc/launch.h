@@ -18,7 +18,8 @@ extern "C" {
 int mgb_launch_set_bc(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_add_du(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_copy(int n, const double *const *src, double *const *dst, const int *list, int nlist, cudaStream_t s);
-// ref_order: form the element residual terms in the reference's order (the FP64 form).
+// ref_order: the element residual by B-matrix products in the reference's order (the FP64 form); otherwise by
+// sum factorisation (the mixed form).
 int mgb_launch_residual(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, int nlist, int ref_order, cudaStream_t s);
 int mgb_launch_assembly(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
