@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -44,7 +45,27 @@ typedef struct {
   long cost;
   int converged, subiterated, coupling;
   int nr_its, nr_solver_its, nr_converged;
+  double op_count[ORC_NOPS], op_sec[ORC_NOPS]; /* instrumentation only (orc_get_ops) */
 } orc_gp;
+
+/* Operation record of the Gauss point whose homogenization runs on this thread (NULL: not recorded).  It
+ * only counts and times operations; no result depends on it. */
+static __thread orc_gp *t_ops;
+
+static double wtime(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return (double)clock() / CLOCKS_PER_SEC;
+#endif
+}
+
+static void op_add(int op, double count, double t0) {
+  if (t_ops) {
+    t_ops->op_count[op] += count;
+    t_ops->op_sec[op] += wtime() - t0;
+  }
+}
 
 typedef struct {
   int n[3], nn, nrow;
@@ -522,8 +543,110 @@ static double get_dot(const double *a, const double *b, int n) {
 #endif
 }
 
+#ifdef ORC_GPU_ORDER
+/* With -DORC_GPU_ORDER the CG's dot products are summed in the order of the GB300 library's FP64 CG kernels:
+ * per-thread partials (one node of 3 rows per thread in the set-up and the SpMV, 4 rows strided by the grid
+ * per thread in the update), 256-thread blocks, shuffle-down warp trees, a tree over the 8 warp sums, and the
+ * last block adding the block partials strided by its 256 threads before one more block tree.  That build only
+ * serves to measure how much a different summation order moves the results (tests/test_rounding_floor.py). */
+#define GPU_BLOCK 256
+#define GPU_UPD_ROWS 4
+
+static double warp_tree(double w[32]) {
+  for (int o = 16; o > 0; o >>= 1)
+    for (int l = 0; l < 32; ++l) w[l] = w[l] + (l + o < 32 ? w[l + o] : w[l]);
+  return w[0];
+}
+
+static double block_tree(const double *t, long n) {
+  double sh[32];
+  for (int wi = 0; wi < 32; ++wi) sh[wi] = 0.0;
+  for (int wi = 0; wi < GPU_BLOCK / 32; ++wi) {
+    double w[32];
+    for (int l = 0; l < 32; ++l) w[l] = (wi * 32 + l < n) ? t[wi * 32 + l] : 0.0;
+    sh[wi] = warp_tree(w);
+  }
+  return warp_tree(sh);
+}
+
+/* Sum of per-thread partials part[0..nthreads) by the grid tree. */
+static double grid_tree(const double *part, long nthreads) {
+  const long nb = (nthreads + GPU_BLOCK - 1) / GPU_BLOCK;
+  double *red = (double *)malloc(nb * sizeof(double));
+  for (long b = 0; b < nb; ++b) {
+    const long rem = nthreads - b * GPU_BLOCK;
+    red[b] = block_tree(part + b * GPU_BLOCK, rem < GPU_BLOCK ? rem : GPU_BLOCK);
+  }
+  double acc[GPU_BLOCK];
+  for (int t = 0; t < GPU_BLOCK; ++t) {
+    acc[t] = 0.0;
+    for (long b = t; b < nb; b += GPU_BLOCK) acc[t] += red[b];
+  }
+  free(red);
+  return block_tree(acc, GPU_BLOCK);
+}
+
+static int node_on_boundary(const orc_ell *m, int n) {
+  const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
+  return on_boundary(n % nx, (n / nx) % ny, n / (nx * ny), nx, ny, nz);
+}
+
+/* r.z and z.z of the CG set-up, one node per thread. */
+static void gpu_setup_dots(const orc_ell *m, const double *r, const double *z, double *rz, double *zz) {
+  const long nt = (long)((m->nn + GPU_BLOCK - 1) / GPU_BLOCK) * GPU_BLOCK;
+  double *a = (double *)calloc(nt, sizeof(double)), *b = (double *)calloc(nt, sizeof(double));
+  for (int n = 0; n < m->nn; ++n)
+    for (int d = 0; d < 3; ++d) {
+      a[n] += r[n * 3 + d] * z[n * 3 + d];
+      b[n] += z[n * 3 + d] * z[n * 3 + d];
+    }
+  *rz = grid_tree(a, nt);
+  *zz = grid_tree(b, nt);
+  free(a);
+  free(b);
+}
+
+/* p.Ap of the SpMV, one node per thread: p0 y0 + p1 y1 + p2 y2 inside, p.p on boundary nodes. */
+static double gpu_spmv_dot(const orc_ell *m, const double *p, const double *y) {
+  const long nt = (long)((m->nn + GPU_BLOCK - 1) / GPU_BLOCK) * GPU_BLOCK;
+  double *a = (double *)calloc(nt, sizeof(double));
+  for (int n = 0; n < m->nn; ++n) {
+    const double *q = p + n * 3, *w = y + n * 3;
+    if (node_on_boundary(m, n)) {
+      for (int d = 0; d < 3; ++d) a[n] += q[d] * q[d];
+    } else {
+      a[n] = q[0] * w[0] + q[1] * w[1] + q[2] * w[2];
+    }
+  }
+  const double s = grid_tree(a, nt);
+  free(a);
+  return s;
+}
+
+/* z.z and r.z of the update: GPU_UPD_ROWS rows per thread, strided by the grid. */
+static void gpu_update_dots(const orc_ell *m, const double *r, const double *z, double *zz, double *rz) {
+  const long per = (long)GPU_UPD_ROWS * GPU_BLOCK;
+  const long nb = (m->nrow + per - 1) / per, nt = nb * GPU_BLOCK, stride = nt;
+  double *a = (double *)calloc(nt, sizeof(double)), *b = (double *)calloc(nt, sizeof(double));
+  for (long t = 0; t < nt; ++t)
+    for (long row0 = t; row0 < m->nrow; row0 += GPU_UPD_ROWS * stride)
+      for (int q = 0; q < GPU_UPD_ROWS; ++q) {
+        const long row = row0 + q * stride;
+        if (row < m->nrow) {
+          a[t] += z[row] * z[row];
+          b[t] += r[row] * z[row];
+        }
+      }
+  *zz = grid_tree(a, nt);
+  *rz = grid_tree(b, nt);
+  free(a);
+  free(b);
+}
+#endif
+
 /* ell_solve_cgpd (ell.cpp:66-122): Jacobi-preconditioned CG from x0 = 0, stopping on ||z||. */
 static int ell_solve_cgpd(orc_ell *m, const double *b, double *x, double *err) {
+  double t0 = wtime();
   for (int i = 0; i < m->nn; i++)
     for (int d = 0; d < 3; d++) m->k[i * 3 + d] = 1 / m->vals[(size_t)i * 3 * NNZ + 13 * 3 + d * NNZ + d];
   for (int i = 0; i < m->nrow; ++i) x[i] = 0.0;
@@ -531,25 +654,44 @@ static int ell_solve_cgpd(orc_ell *m, const double *b, double *x, double *err) {
   for (int i = 0; i < m->nrow; ++i) m->r[i] = b[i] - m->r[i];
   for (int i = 0; i < m->nrow; ++i) m->z[i] = m->k[i] * m->r[i];
   for (int i = 0; i < m->nrow; ++i) m->p[i] = m->z[i];
+#ifdef ORC_GPU_ORDER
+  double rz, zz0;
+  gpu_setup_dots(m, m->r, m->z, &rz, &zz0);
+  const double pnorm_0 = sqrt(zz0);
+#else
   double rz = get_dot(m->r, m->z, m->nrow);
   const double pnorm_0 = sqrt(get_dot(m->z, m->z, m->nrow));
+#endif
   double pnorm = pnorm_0;
   int its = 0;
+  op_add(ORC_OP_CG_SETUP, 1, t0);
+  t0 = wtime();
   while (its < m->max_its) {
     if (pnorm < m->min_err || pnorm < pnorm_0 * m->rel_err) break;
     ell_mvp(m, m->p, m->Ap);
+#ifdef ORC_GPU_ORDER
+    const double pAp = gpu_spmv_dot(m, m->p, m->Ap);
+#else
     const double pAp = get_dot(m->p, m->Ap, m->nrow);
+#endif
     const double alpha = rz / pAp;
     for (int i = 0; i < m->nrow; ++i) x[i] += alpha * m->p[i];
     for (int i = 0; i < m->nrow; ++i) m->r[i] -= alpha * m->Ap[i];
     for (int i = 0; i < m->nrow; ++i) m->z[i] = m->k[i] * m->r[i];
+#ifdef ORC_GPU_ORDER
+    double zz, rz_n;
+    gpu_update_dots(m, m->r, m->z, &zz, &rz_n);
+    pnorm = sqrt(zz);
+#else
     pnorm = sqrt(get_dot(m->z, m->z, m->nrow));
     const double rz_n = get_dot(m->r, m->z, m->nrow);
+#endif
     const double beta = rz_n / rz;
     for (int i = 0; i < m->nrow; ++i) m->p[i] = m->z[i] + beta * m->p[i];
     rz = rz_n;
     its++;
   }
+  op_add(ORC_OP_CG_ITER, its, t0);
   *err = rz;
   return its;
 }
@@ -631,6 +773,7 @@ static void get_elem_rhs(const orc_rve *h, const double *u, const double *vars, 
 
 /* assembly_rhs (assembly.cpp:27-103): b = -(sum_e be) with Dirichlet rows zeroed; returns ||b||_2. */
 static double assembly_rhs(const orc_rve *h, const double *u, const double *vars, double *b) {
+  const double t0 = wtime();
   const int nx = h->nx, ny = h->ny, nz = h->nz, nxny = nx * ny;
   memset(b, 0, h->nndim * sizeof(double));
   for (int ez = 0; ez < h->nez; ++ez)
@@ -651,6 +794,7 @@ static double assembly_rhs(const orc_rve *h, const double *u, const double *vars
   for (int i = 0; i < h->nndim; ++i) b[i] = -b[i];
   double norm = 0.0;
   for (int i = 0; i < h->nndim; ++i) norm += b[i] * b[i];
+  op_add(ORC_OP_RESIDUAL, 1, t0);
   return sqrt(norm);
 }
 
@@ -681,19 +825,33 @@ static void get_elem_mat(const orc_rve *h, const double *u, const double *vars, 
 
 /* assembly_mat (assembly.cpp:105-121); note the ex-outer loop order. */
 static void assembly_mat(const orc_rve *h, orc_ell *A, const double *u, const double *vars) {
+  const double t0 = wtime();
   memset(A->vals, 0, (size_t)A->nrow * NNZ * sizeof(double));
   double Ae[NPEDIM * NPEDIM];
+#ifdef ORC_GPU_ORDER
+  /* the GB300 library's order: 8 colours by the parity of (ex, ey, ez), colour c = cx + 2 cy + 4 cz */
+  for (int c = 0; c < 8; ++c)
+    for (int ez = (c >> 2) & 1; ez < h->nez; ez += 2)
+      for (int ey = (c >> 1) & 1; ey < h->ney; ey += 2)
+        for (int ex = c & 1; ex < h->nex; ex += 2) {
+          get_elem_mat(h, u, vars, Ae, ex, ey, ez);
+          ell_add_3d(A, ex, ey, ez, Ae);
+        }
+#else
   for (int ex = 0; ex < h->nex; ++ex)
     for (int ey = 0; ey < h->ney; ++ey)
       for (int ez = 0; ez < h->nez; ++ez) {
         get_elem_mat(h, u, vars, Ae, ex, ey, ez);
         ell_add_3d(A, ex, ey, ez, Ae);
       }
+#endif
   ell_set_bc_3d(A);
+  op_add(ORC_OP_ASSEMBLY, 1, t0);
 }
 
 /* calc_ave_stress (average.cpp:57-82). */
 static void calc_ave_stress(const orc_rve *h, const double *u, double ave[6], const double *vars) {
+  const double t0 = wtime();
   memset(ave, 0, 6 * sizeof(double));
   for (int ez = 0; ez < h->nez; ++ez)
     for (int ey = 0; ey < h->ney; ++ey)
@@ -709,10 +867,12 @@ static void calc_ave_stress(const orc_rve *h, const double *u, double ave[6], co
         for (int v = 0; v < 6; ++v) ave[v] += aux[v];
       }
   for (int v = 0; v < 6; ++v) ave[v] /= h->vol_tot;
+  op_add(ORC_OP_AVE_STRESS, 1, t0);
 }
 
 /* calc_vars_new (update.cpp:32-56). */
 static int calc_vars_new(const orc_rve *h, const double *u, const double *vold, double *vnew) {
+  const double t0 = wtime();
   int nl = 0;
   for (int ez = 0; ez < h->nez; ++ez)
     for (int ey = 0; ey < h->ney; ++ey)
@@ -725,6 +885,7 @@ static int calc_vars_new(const orc_rve *h, const double *u, const double *vold, 
                             &vnew[(size_t)e * NPE * NVAR_GP + gp * NVAR_GP]);
         }
       }
+  op_add(ORC_OP_VARS, 1, t0);
   return nl;
 }
 
@@ -782,6 +943,8 @@ static void homogenize_linear_gp(orc_gp *g) {
 /* homogenize_fe_one_way / homogenize_fe_full (homogenize.cpp:111-282).  They differ only in the final
  * ctan block, which runs for FE_FULL. */
 static void homogenize_fe(const orc_rve *h, orc_gp *g, int full) {
+  const double t_start = wtime();
+  t_ops = g;
   orc_ell A;
   const int ns[3] = {h->nx, h->ny, h->nz};
   ell_init(&A, ns, h->cg_abs_tol, h->cg_rel_tol, h->cg_max_its);
@@ -852,6 +1015,8 @@ static void homogenize_fe(const orc_rve *h, orc_gp *g, int full) {
   free(u);
   free(du);
   free(vars_new_aux);
+  op_add(ORC_OP_HOMOGENIZE, 1, t_start);
+  t_ops = NULL;
 }
 
 /* calc_ctan_lin_fe_models (micropp.cpp:255-284). */
@@ -1100,6 +1265,16 @@ void orc_get_u(const orc_rve *h, int gp, int which, double *out) {
     memcpy(out, src, h->nndim * sizeof(double));
   else
     memset(out, 0, h->nndim * sizeof(double));
+}
+void orc_get_ops(const orc_rve *h, int gp, double *count, double *sec) {
+  memcpy(count, h->gp[gp].op_count, sizeof(h->gp[gp].op_count));
+  memcpy(sec, h->gp[gp].op_sec, sizeof(h->gp[gp].op_sec));
+}
+void orc_reset_ops(orc_rve *h) {
+  for (int i = 0; i < h->ngp; ++i) {
+    memset(h->gp[i].op_count, 0, sizeof(h->gp[i].op_count));
+    memset(h->gp[i].op_sec, 0, sizeof(h->gp[i].op_sec));
+  }
 }
 void orc_get_newton(const orc_rve *h, int gp, int *its, int *sits, int *conv) {
   *its = h->gp[gp].nr_its;

@@ -88,6 +88,15 @@ void orc_get_vars(const orc_rve *h, int gp, int which, double *out);
 void orc_get_u(const orc_rve *h, int gp, int which, double *out);
 /* Newton statistics of the most recent main solve of `gp`: its, solver_its, converged. */
 void orc_get_newton(const orc_rve *h, int gp, int *its, int *solver_its, int *converged);
+/* Operation counts and host seconds of every FE homogenization of `gp` since construction or the last
+ * orc_reset_ops, indexed by ORC_OP_*: residual assemblies (assembly_rhs), Jacobian assemblies (assembly_mat),
+ * CG set-ups (one per solve), CG iterations, average stresses, internal-variable updates, and whole
+ * homogenize_fe calls (whose seconds include everything, also allocation and copies).  Instrumentation for
+ * the CPU baseline's cost model; no result depends on it. */
+enum { ORC_OP_RESIDUAL, ORC_OP_ASSEMBLY, ORC_OP_CG_SETUP, ORC_OP_CG_ITER, ORC_OP_AVE_STRESS, ORC_OP_VARS,
+       ORC_OP_HOMOGENIZE, ORC_NOPS };
+void orc_get_ops(const orc_rve *h, int gp, double *count, double *sec);
+void orc_reset_ops(orc_rve *h);
 /* Restart files in the reference's binary format (gp.hpp:107-124, output.cpp:216-262). */
 int orc_write_restart(const orc_rve *h, const char *path);
 int orc_read_restart(orc_rve *h, const char *path);

@@ -231,7 +231,20 @@ class OracleRVE(_Base):
             L.orc_read_restart.argtypes = [C.c_void_p, C.c_char_p]
             L.orc_read_restart.restype = C.c_int
             L.orc_calc_bmat.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double)]
+            L.orc_get_ops.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.orc_reset_ops.argtypes = [C.c_void_p]
         super().__init__(cfg)
+
+    OPS = ("residual", "assembly", "cg_setup", "cg_iter", "ave_stress", "vars", "homogenize")
+
+    def ops(self, gp):
+        """{op: (count, seconds)} of the FE homogenizations of `gp` since construction or reset_ops()."""
+        cnt, sec = (C.c_double * 7)(), (C.c_double * 7)()
+        self.lib.orc_get_ops(self.h, gp, cnt, sec)
+        return {k: (cnt[i], sec[i]) for i, k in enumerate(self.OPS)}
+
+    def reset_ops(self):
+        self.lib.orc_reset_ops(self.h)
 
     def newton(self, gp):
         a, b, c = C.c_int(), C.c_int(), C.c_int()
