@@ -44,7 +44,37 @@ def case(name):
                   coupling=[2], lin_stress=0, nr_max_its=30, nr_max_tol=1e-5)
         steps = [[np.array([1e-2, 0, 0, 0, 0, 0]) * s / 4] for s in range(1, 5)]
         return kw, steps
+    if name == "c1_sphere_elastic_cg1e8":
+        # The C1 case at the CG tolerance its configuration states (1e-8).  The reference hard-wires
+        # CG_REL_TOL (ell.hpp:35), so its fixture comes from the reference compiled with that define at 1e-8;
+        # the oracle and the library take the tolerance as cg_rel_tol.
+        kw, steps = case("c1_sphere_elastic")
+        kw["cg_rel_tol"] = 1e-8
+        return kw, steps
+    if name == "linear_full":
+        # FE_LINEAR points (stress = ctan_lin strain, homogenize.cpp:51-66,101-109) next to an FE_FULL point
+        # on a damage matrix: the dispatch of homogenize.cpp:68-99 over mixed couplings.
+        n = 6
+        kw = dict(n=n, ngp=3, micro_type=1, geo=(0.25, 0, 0, 0),
+                  mats=((2, 1e7, 0.25, 0, 0, 1e5), (0, 1e8, 0.25, 0, 0, 0), (0, 1e7, 0.25, 0, 0, 0)),
+                  coupling=[0, 2, 0], lin_stress=0, nr_max_its=12, nr_max_tol=1e-5)
+        base = np.array([2e-2, -6e-3, 0, 1e-2, 0, 0])
+        steps = [[base * s / 2, base * s / 2, -0.5 * base * s / 2] for s in (1, 2)]
+        return kw, steps
     raise KeyError(name)
+
+
+# Cases whose reference fixture comes from a compiled-reference variant other than the stock build.
+REF_VARIANT = {"c1_sphere_elastic_cg1e8": "cg1e8"}
+
+
+def linear_pass(name):
+    """Strains of a final micropp3_homogenize_linear call (stress = ctan strain for every point, whatever its
+    coupling; homogenize.cpp:51-66), made after the case's steps; None where the case has none."""
+    if name == "linear_full":
+        rng = np.random.default_rng(7)
+        return [rng.uniform(-1e-2, 1e-2, 6) for _ in range(3)]
+    return None
 
 
 def split_kw(kw):

@@ -5,11 +5,12 @@
    files, together with the outputs of the compiled reference (oracle/_ref) on the same 10-step paths.
 2. ref_<case>.npz -- outputs of the compiled reference on the seeded parity cases of tests/cases.py:
    per step and Gauss point the average stress, ctan, cost, flags, and the internal variables and the
-   displacement of the last step.
+   displacement of the last step; for cases with a final homogenize_linear pass, its stresses.  The case
+   c1_sphere_elastic_cg1e8 comes from the reference built with CG_REL_TOL = 1e-8 (libref_cg1e8).
 3. ref_output_damage.vtu -- the reference's VTU field output (micropp<3>::output) of a 3^3 damage RVE after
    one nonlinear step, and ref_output_j2.vtu for a J2 matrix.
 
-Usage: python tests/golden/make_golden.py [reference_root]   (needs oracle/build_ref.sh to have run)
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT   (or MICROPP_REFERENCE; needs oracle/build_ref.sh)
 """
 import json
 import os
@@ -58,10 +59,10 @@ def run_table_case(material):
 
 
 def run_case(name):
-    from cases import case, oracle_config, split_kw
+    from cases import REF_VARIANT, case, linear_pass, oracle_config, split_kw
     kw, steps = case(name)
     n, kw2 = split_kw(kw)
-    r = orc.RefRVE(oracle_config(n, **kw2))
+    r = orc.RefRVE(oracle_config(n, **kw2), variant=REF_VARIANT.get(name, "stock"))
     rec = {"stress": [], "ctan": [], "cost": [], "converged": [], "nonlinear": []}
     for st in steps:
         for gp, e in enumerate(st):
@@ -80,6 +81,12 @@ def run_case(name):
     arrays["vars_k_last"] = np.array(last_vars)
     arrays["u_k_last"] = np.array(last_u)
     arrays["ctan_lin"] = r.ctan_lin()
+    lin = linear_pass(name)
+    if lin is not None:
+        for gp, e in enumerate(lin):
+            r.set_strain(gp, e)
+        r.homogenize_linear()
+        arrays["stress_linear"] = np.array([r.get_stress(g) for g in range(len(lin))])
     r.close()
     np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **arrays)
 
@@ -95,7 +102,9 @@ def vtu_cases():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MICROPP_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT  (or set MICROPP_REFERENCE)")
     tables = {}
     for key in ("elastic", "plastic", "damage"):
         sig, tol, material = parse_table(os.path.join(ref, "test", f"benchmark-{key}.cpp"))
@@ -103,7 +112,8 @@ def main():
                        "ref_output": run_table_case(material)}
     with open(os.path.join(HERE, "benchmark_tables.json"), "w") as f:
         json.dump(tables, f, indent=1)
-    for name in ("c1_sphere_elastic", "damage_layers", "plastic_sphere"):
+    for name in ("c1_sphere_elastic", "damage_layers", "plastic_sphere", "c1_sphere_elastic_cg1e8",
+                 "linear_full"):
         run_case(name)
     for tag, cfg_kw, eps in vtu_cases():
         r = orc.RefRVE(orc.make_config(3, **cfg_kw))

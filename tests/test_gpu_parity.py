@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import pyoracle as orc
-from cases import case, gpu_config, oracle_config, split_kw
+from cases import case, gpu_config, linear_pass, oracle_config, split_kw
 from conftest import rel_err
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +60,38 @@ def run_pair(name, gpu_lib, check_vars=True, cost_exact=True, tol_ctan=TOL_CTAN)
 
 def test_c1_sphere_elastic(gpu_lib):
     run_pair("c1_sphere_elastic", gpu_lib)
+
+
+def test_c1_sphere_elastic_cg_tol_1e8(gpu_lib):
+    """C1 at its stated CG tolerance 1e-8 (cg_rel_tol), against the oracle and the fixture of the reference
+    compiled with CG_REL_TOL = 1e-8 (ell.hpp:35)."""
+    import os
+    g, _ = run_pair("c1_sphere_elastic_cg1e8", gpu_lib)
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_c1_sphere_elastic_cg1e8.npz"))
+    assert rel_err(g.get_stress(0), ref["stress"][-1][0]) < TOL_STRESS
+    assert g.get_cost(0) == ref["cost"][-1][0] == 32
+    assert rel_err(g.ctan_lin(), ref["ctan_lin"]) < TOL_CTAN_LIN
+
+
+def test_fe_linear_next_to_fe_full_and_homogenize_linear(gpu_lib):
+    """FE_LINEAR points (stress = ctan_lin strain, no FE solve, cost 0) beside an FE_FULL damage point
+    (homogenize.cpp:68-99), then micropp3_homogenize_linear over all points (homogenize.cpp:51-66): against
+    the oracle and the compiled reference's fixture."""
+    import os
+    g, o = run_pair("linear_full", gpu_lib)
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_linear_full.npz"))
+    assert [g.get_cost(gp) for gp in range(3)] == [0, ref["cost"][-1][1], 0]
+    lin = linear_pass("linear_full")
+    for gp, e in enumerate(lin):
+        g.set_strain(gp, e)
+        o.set_strain(gp, e)
+    g.homogenize_linear()
+    o.homogenize_linear()
+    for gp in range(3):
+        assert rel_err(g.get_stress(gp), o.get_stress(gp)) < TOL_STRESS
+        assert rel_err(g.get_stress(gp), ref["stress_linear"][gp]) < TOL_STRESS
+        # the linear pass leaves ctan as it was
+        assert rel_err(g.get_ctan(gp), o.get_ctan(gp)) < (TOL_CTAN if o.is_non_linear(gp) else TOL_CTAN_LIN)
 
 
 def test_damage_layers_two_points(gpu_lib):

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import pyoracle as orc
-from cases import case, oracle_config, split_kw
+from cases import case, linear_pass, oracle_config, split_kw
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -37,9 +37,12 @@ def test_reference_golden_tables(key):
     assert np.array_equal(sig, np.array(g["ref_output"]))  # bit-for-bit with the compiled reference
 
 
-@pytest.mark.parametrize("name", ["c1_sphere_elastic", "damage_layers", "plastic_sphere"])
+@pytest.mark.parametrize("name", ["c1_sphere_elastic", "damage_layers", "plastic_sphere", "c1_sphere_elastic_cg1e8",
+                                  "linear_full"])
 def test_reference_fixtures(name):
-    """Seeded FE_FULL cases: stress, ctan, cost, flags, history and displacement equal the reference's."""
+    """Seeded cases: stress, ctan, cost, flags, history and displacement equal the reference's.  The cg1e8 case
+    is pinned to the reference compiled with CG_REL_TOL = 1e-8 (the oracle takes it as cg_rel_tol); the
+    linear_full case mixes FE_LINEAR and FE_FULL points and ends with a homogenize_linear pass."""
     ref = np.load(os.path.join(GOLD, f"ref_{name}.npz"))
     kw, steps = case(name)
     n, kw2 = split_kw(kw)
@@ -59,6 +62,13 @@ def test_reference_fixtures(name):
                 assert np.array_equal(r.vars(gp, 1), ref["vars_k_last"][gp])
                 assert np.array_equal(r.u(gp, 1), ref["u_k_last"][gp])
         r.update_vars()
+    lin = linear_pass(name)
+    if lin is not None:
+        for gp, e in enumerate(lin):
+            r.set_strain(gp, e)
+        r.homogenize_linear()
+        for gp in range(len(lin)):
+            assert np.array_equal(r.get_stress(gp), ref["stress_linear"][gp])
 
 
 needs_ref = pytest.mark.skipif(not orc.ref_available(), reason="compiled reference (oracle/_ref) not built here")
