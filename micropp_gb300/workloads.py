@@ -68,3 +68,27 @@ def monotone_path(target, steps):
 
 def random_targets(count, seed, amp):
     return np.random.default_rng(seed).uniform(-amp, amp, size=(count, 6))
+
+
+def damage_layers_rves(n, rves, seed):
+    """The headline workload's RVEs: phase map (4 layers normal to z), damage thresholds and seeded strain
+    targets ~ U[-2.5e-2, 2.5e-2]^6.
+
+    The reference's damage law is continuous at first loading only for Xt = 1e5, its hard-wired Ey
+    (material.cpp:205-268): a larger Xt makes the stress jump by q(r)/r (5x at Xt = 2.35e5) and a smaller
+    one fully damages points (NaN).  Every RVE therefore uses Xt = 1e5; the RVEs differ by their seeded
+    strain targets."""
+    xts = np.full(rves, 1e5)
+    targets = random_targets(rves, seed + 1, 2.5e-2)
+    return layers_z(n), xts, targets
+
+
+def damage_layers_materials(mg, xt=1e5):
+    """Materials of the headline workload: damage matrix (E = 1e7, nu = 0.25, Xt), stiff elastic layers
+    (E = 1e8, nu = 0.25); `mg` is the micropp_gb300 module."""
+    return [mg.material(2, 1e7, 0.25, 0, 0, xt), mg.material(0, 1e8, 0.25), mg.material(0, 1e7, 0.25)]
+
+
+# Options of the fast form of the headline: FP32 Jacobian and multigrid-preconditioned CG inside FP64
+# refinement, Newton to 1e-8 of its initial residual, ctan by implicit differentiation.
+FAST_FORM = dict(precision=1, ctan_mode=1, nr_max_its=20, nr_max_tol=1e-30, nr_rel_tol=1e-8, precond=1)
