@@ -156,9 +156,11 @@ int micropp3_ell_solve_cgpd(const int nodes[3], const double *vals, const double
  * on the allocator).  This entry point has no counterpart in the reference.  Its work vectors live in one
  * fixed array of device memory that the library holds on every GPU where it is loaded, until the process
  * exits (about 16 MB), so the grid may have at most MICROPP3_NOALLOC_MAX_NODES nodes (50 x 50 x 50);
- * larger grids return -3.  The caller passes vals, b and x as for micropp3_ell_solve_cgpd.  The first call on
- * a device resolves the array's address on that device; make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU (other host threads, other streams) race and must be serialised.
+ * larger grids return -3.  The caller passes vals, b and x as for micropp3_ell_solve_cgpd.  Each call looks
+ * up the array's address on the current device; the first call on a device also loads the library's device
+ * code there, so make it before any stream capture.  The call returns when the solve has finished (it
+ * synchronises the stream).  All calls share the array and find the previous call's data in it: calls that
+ * overlap on the GPU (other host threads, other streams) race and must be serialised.
  * Returns 0, -1 for invalid arguments, -3 for a grid over the limit, or the CUDA error code. */
 #define MICROPP3_NOALLOC_MAX_NODES 131072
 int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double *vals, const double *b, double *x,

@@ -20,11 +20,6 @@ namespace mgb {
 
 namespace {
 
-struct CudaFailure : std::runtime_error {
-  cudaError_t code;
-  CudaFailure(cudaError_t c, const char *what) : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {}
-};
-
 void chk(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaFailure(e, what);
 }

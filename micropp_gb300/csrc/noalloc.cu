@@ -10,16 +10,18 @@
 // elements); the array holds five work vectors of 3 * 131,072 doubles plus the reduction partials and a few
 // counters, about 16.3 MB.
 //
-// Sharing: every call uses the same array and leaves its contents behind; the counters that must start at
-// zero are cleared at the start of each call.  Two calls whose work overlaps on the GPU -- from two host
-// threads, or on two streams -- race on the array and give wrong results; serialise them.
+// Sharing: every call uses the same array and leaves its contents behind; the counters and the result record
+// that must start at zero are cleared at the start of each call.  Two calls whose work overlaps on the GPU --
+// from two host threads, or on two streams -- race on the array and give wrong results; serialise them.
 //
-// Set-up: the first call on a device resolves the device address of the array (cudaGetSymbolAddress, with
-// that device current) and keeps it for later calls; make that first call before any stream capture.
+// Set-up: each call resolves the device address of the array on the current device (cudaGetSymbolAddress)
+// before it launches anything.  The address is not cached: a cudaDeviceReset or a re-created primary context
+// reloads the library's device code and moves the array, and a kept address would then point at freed
+// memory.  The first call on a device also loads the device code there; make that first call before any
+// stream capture.  The call returns once the solve has finished (it synchronises the stream).
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 #include <stdexcept>
 
 #include "device.cuh"
@@ -54,23 +56,13 @@ __global__ void k_noalloc_clear(unsigned int *ticket, unsigned int *count) {
   }
 }
 
-std::mutex g_setup_mutex;
-unsigned char *g_scratch_addr[64] = {nullptr};
-
-// Device address of g_noalloc_scratch on the current device (resolved once per device).
+// Device address of g_noalloc_scratch in the current context.  In host code the symbol's own name is a
+// host-side stand-in, not a device address, so kernels are given only what this returns.
 cudaError_t scratch_address(unsigned char **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = (unsigned char *)p;
-  }
-  *out = g_scratch_addr[dev];
+  *out = (unsigned char *)p;
   return cudaSuccess;
 }
 
@@ -116,16 +108,15 @@ extern "C" int micropp3_ell_solve_cgpd_noalloc(const int nodes[3], const double 
   try {
     k_noalloc_clear<<<1, 32, 0, s>>>(I.ticket, d_count);
     e = cudaGetLastError();
-    if (e != cudaSuccess) return (int)e;
-    e = cudaMemcpyAsync(d_inst, &I, sizeof(Inst), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(I.out, 0, sizeof(InstOut), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_inst, &I, sizeof(Inst), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_list, &zero, sizeof(int), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return (int)e;
     const int n = run_dpcg(m, d_inst, d_list, d_count, I.cg, I.out, rel_tol, abs_tol, max_its, s);
     if (its) *its = n;
-  } catch (const std::exception &ex) {
-    std::fprintf(stderr, "micropp3_ell_solve_cgpd_noalloc: %s\n", ex.what());
-    e = cudaGetLastError();
-    return e != cudaSuccess ? (int)e : -2;
+  } catch (const CudaFailure &f) {
+    std::fprintf(stderr, "micropp3_ell_solve_cgpd_noalloc: %s\n", f.what());
+    return (int)f.code;
   }
   return 0;
 }
