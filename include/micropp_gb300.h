@@ -38,11 +38,14 @@ enum {
  * tangent solve). */
 enum {
   MICROPP3_PRECOND_JACOBI = 0, /* point Jacobi, as the reference's DPCG (default) */
-  MICROPP3_PRECOND_MG = 1      /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
-                                * damped-Jacobi smoothing; every axis coarsens to ceil(elements / 2).  Needs at
-                                * least 4 elements along every axis and more than 4 along one.  On strongly
-                                * anisotropic tangents (loading damage, J2 plastic flow) its CG can stall where
-                                * Jacobi's converges. */
+  MICROPP3_PRECOND_MG = 1,     /* geometric multigrid V-cycle: trilinear transfers, Galerkin coarse operators,
+                                * Jacobi smoothing with the safeguarded diagonal max(a_ii / 0.6, 0.55 sum_j
+                                * |a_ij|); every axis coarsens to ceil(elements / 2).  Needs at least 4 elements
+                                * along every axis and more than 4 along one.  A solve that reaches 100
+                                * iterations is redone with Jacobi. */
+  MICROPP3_PRECOND_MG_HALF = 2 /* MICROPP3_PRECOND_MG whose two fine-level smoothing passes read an FP16 copy of
+                                * the fine operator (scaled by a power of two), half the bytes of the FP32 values;
+                                * the CG itself keeps the FP32 operator */
 };
 
 /* Per-RVE status word of the last homogenize(). */

@@ -23,7 +23,7 @@ MATERIAL_ELASTIC, MATERIAL_PLASTIC, MATERIAL_DAMAGE = 0, 1, 2
  MIC3D_FIBS_20_DISORDER) = range(13)
 FP64, MIXED = 0, 1
 CTAN_PERTURB, CTAN_IMPLICIT = 0, 1
-PRECOND_JACOBI, PRECOND_MG = 0, 1
+PRECOND_JACOBI, PRECOND_MG, PRECOND_MG_HALF = 0, 1, 2
 STATUS_OK, STATUS_NEWTON_MAX_ITS, STATUS_CG_MAX_ITS, STATUS_NONFINITE = 0, 1, 2, 4
 
 

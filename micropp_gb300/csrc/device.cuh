@@ -69,6 +69,7 @@ struct Cg6State {
   double rz[6], pnorm0[6], pnorm[6], alpha[6], beta[6];
   double min_err, rel_err;
   int its, max_its, done[6], all_done, pad;
+  double ecorr[36];  // interior term of the energy form of ctan, sum over interior nodes of x_k . RF_i ([k * 6 + i])
 };
 
 // Small per-instance outputs read back by the host.
@@ -101,6 +102,9 @@ struct MgLevel {
 struct MgInst {
   MgLevel lv[kMgMaxLevels];
   float *mid1, *mid2;      // the separable Galerkin product's intermediate operators (x, then x and y coarsened)
+  unsigned short *vals16;  // FP16 bits of scale16 x the level-0 operator (MICROPP3_PRECOND_MG_HALF), else NULL
+  float scale16, inv16;    // a power of two and its inverse
+  int pad[2];
 };
 
 struct Inst {

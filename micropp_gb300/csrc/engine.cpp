@@ -34,6 +34,10 @@ constexpr double kDepsCtanAve = 1.0e-8;        // params.hpp:32
 // until ||f_i - K x_i|| <= kTangentTol ||f_i|| for all six right-hand sides (at most kTangentSweeps sweeps).
 constexpr double kTangentSweepRel = 1.0e-5;
 constexpr double kTangentTol = 1.0e-9;
+// With a symmetric tangent (every phase elastic or damage) ctan takes the energy form, whose error is quadratic
+// in the solve's: the sweeps go to 2e-6 and the refinement stops at 3e-6 ||f_i||.
+constexpr double kTangentSweepRelEnergy = 2.0e-6;
+constexpr double kTangentTolEnergy = 3.0e-6;
 constexpr int kTangentSweeps = 4;
 
 // Lowest relative tolerance asked of the mixed form's FP32 Newton CG.
@@ -113,9 +117,12 @@ Engine::Engine(const micropp3_config &cfg) {
   // Multigrid levels: every axis of n elements coarsens to ceil(n / 2) while each axis keeps at least 4
   // elements and some axis has more than 4.
   {
-    const int pc = cfg.precond;
-    if (pc != MICROPP3_PRECOND_JACOBI && pc != MICROPP3_PRECOND_MG)
-      throw std::invalid_argument("precond must be MICROPP3_PRECOND_JACOBI or MICROPP3_PRECOND_MG");
+    const int pc0 = cfg.precond;
+    if (pc0 != MICROPP3_PRECOND_JACOBI && pc0 != MICROPP3_PRECOND_MG && pc0 != MICROPP3_PRECOND_MG_HALF)
+      throw std::invalid_argument("precond must be MICROPP3_PRECOND_JACOBI, MICROPP3_PRECOND_MG or "
+                                  "MICROPP3_PRECOND_MG_HALF");
+    mg_half_ = pc0 == MICROPP3_PRECOND_MG_HALF;
+    const int pc = mg_half_ ? MICROPP3_PRECOND_MG : pc0;
     const bool fp32_solves = precision_ == MICROPP3_MIXED || ctan_mode_ == MICROPP3_CTAN_IMPLICIT;
     if (pc == MICROPP3_PRECOND_MG && !fp32_solves)
       throw std::invalid_argument("the multigrid preconditioner applies to the FP32 solves (MICROPP3_MIXED or "
@@ -133,6 +140,18 @@ Engine::Engine(const micropp3_config &cfg) {
       throw std::invalid_argument("the multigrid preconditioner needs at least 4 elements along every axis and "
                                   "more than 4 along one");
     if (!mg_) mg_mesh_.clear();
+    if (!mg_) mg_half_ = false;
+    if (mg_half_) {
+      // Scale of the FP16 copy: an entry of the fine operator is a sum of at most 8 element blocks; with the
+      // largest entry of the phases' elastic element matrices as the unit, 8 of them map to 2^10, which leaves a
+      // factor 64 below the FP16 maximum for tangents stiffer than elastic (loading damage) and keeps entries
+      // down to 1e-7 of it normal.
+      double kmax = 0.0;
+      for (int ph = 0; ph < 3; ++ph)
+        for (int q = 0; q < 576; ++q) kmax = std::max(kmax, std::fabs(ke_phase_[ph][q]));
+      const double bound = 8.0 * std::max(kmax, 1e-300);
+      mg_scale16_ = (float)std::ldexp(1.0, (int)std::floor(std::log2(1024.0 / bound)));
+    }
   }
 
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
@@ -168,6 +187,8 @@ Engine::Engine(const micropp3_config &cfg) {
   }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
+  check(cudaMallocHost((void **)&h_chunks_, sizeof(unsigned int)), "pinned chunk count");
+  d_chunks_ = dalloc<unsigned int>(1, "chunk count");
 
   gps_.resize(ngp_);
   int n_fe = 0;
@@ -254,6 +275,10 @@ Engine::~Engine() {
   dfree(d_A0_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
+  dfree(d_chunks_);
+  if (h_chunks_) cudaFreeHost(h_chunks_);
+  dfree(d_eta_);
+  if (h_eta_) cudaFreeHost(h_eta_);
   for (cudaEvent_t e : tune_ev_)
     if (e) cudaEventDestroy(e);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -521,6 +546,12 @@ void Engine::ensure_slots(int n) {
         return p;
       };
       h.lv[0].t = buf((size_t)18 * mesh_.np, "multigrid level-0 residual");
+      if (mg_half_) {
+        h.vals16 = dalloc<unsigned short>((size_t)kEllPerNode * mesh_.np, "multigrid FP16 fine operator");
+        w.mg_bufs16.push_back(h.vals16);
+        h.scale16 = mg_scale16_;
+        h.inv16 = 1.0f / mg_scale16_;
+      }
       h.lv[0].kinv = buf((size_t)3 * mesh_.np, "multigrid level-0 smoother diagonal");
       {
         const MeshDev &c = mg_mesh_[1];  // the first product has the largest intermediates
@@ -545,6 +576,14 @@ void Engine::ensure_slots(int n) {
   clear_graphs();  // the captured chunks hold the instance and list pointers
   dfree(d_insts_);
   d_insts_ = dalloc<Inst>(n, "insts");
+  if (eta_cap_ < n) {
+    dfree(d_eta_);
+    if (h_eta_) cudaFreeHost(h_eta_);
+    h_eta_ = nullptr;
+    d_eta_ = dalloc<double>(n, "CG tolerances");
+    check(cudaMallocHost((void **)&h_eta_, n * sizeof(double)), "pinned CG tolerances");
+    eta_cap_ = n;
+  }
   if (h_out_) cudaFreeHost(h_out_);
   check(cudaMallocHost((void **)&h_out_, n * sizeof(InstOut)), "pinned out");
   h_insts_.assign(n, Inst{});
@@ -576,6 +615,8 @@ void Engine::free_slots() {
       dfree(p);
     for (float *p : w.mg_bufs) dfree(p);
     w.mg_bufs.clear();
+    for (unsigned short *p : w.mg_bufs16) dfree(p);
+    w.mg_bufs16.clear();
     dfree(w.mg);
     dfree(w.ticket);
     dfree(w.cg);
@@ -697,10 +738,23 @@ int Engine::tuned_block(int kind, int nlist) {
   return best;
 }
 
+int Engine::known_block(int kind, int nlist) const {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tuned.find(std::make_tuple(kind, mesh_.nn, nlist));
+  return it == g_tuned.end() ? 0 : it->second;
+}
+
+bool Engine::timing_on() const {
+  return t_spmv_.enabled || t_update_.enabled || t_spmv6_.enabled || t_upd6_.enabled || t_mg1_.enabled ||
+         t_asm_.enabled || t_res_.enabled;
+}
+
 void Engine::clear_graphs() {
-  if (!graph_cache_.empty() && stream_) cudaStreamSynchronize(stream_);
+  if ((!graph_cache_.empty() || !newton_graphs_.empty()) && stream_) cudaStreamSynchronize(stream_);
   for (auto &kv : graph_cache_) cudaGraphExecDestroy(kv.second);
   graph_cache_.clear();
+  for (auto &kv : newton_graphs_) cudaGraphExecDestroy(kv.second.exec);
+  newton_graphs_.clear();
 }
 
 void Engine::set_graphs(bool on) {
@@ -930,6 +984,10 @@ void Engine::mg_rap(int nlist) {
   launches_ += 1;
   check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
                "multigrid smoother diagonal");
+  if (mg_half_) {
+    launches_ += 1;
+    check_launch(mgb_launch_mg_half0(&mg_mesh_[0], d_insts_, d_list_, nlist, stream_), "multigrid FP16 operator");
+  }
   for (size_t l = 0; l + 1 < mg_mesh_.size(); ++l) {
     const MeshDev &f = mg_mesh_[l], &c = mg_mesh_[l + 1];
     const MeshDev m1 = grid_of(c.nx, f.ny, f.nz), m2 = grid_of(c.nx, c.ny, f.nz);
@@ -950,7 +1008,8 @@ void Engine::mg_rap(int nlist) {
 // sweeps (one operator pass and three vector passes each); the level-0 restriction and prolongation (three
 // vector passes).
 double Engine::mg_fine_bytes(int nr) const {
-  return 2.0 * (double)nndim() * (81.0 * 4 + 3.0 * nr * 4);
+  const double value_bytes = mg_half_ ? 2.0 : 4.0;  // FP16 copy or FP32 operator
+  return 2.0 * (double)nndim() * (81.0 * value_bytes + 3.0 * nr * 4);
 }
 
 double Engine::mg_coarse_bytes(int nr) const {
@@ -968,13 +1027,15 @@ double Engine::mg_coarse_bytes(int nr) const {
 
 // One V-cycle of the nr-RHS CG of the listed instances (their level-0 iterate x0 = D^-1 r is already
 // written), ending with the level-0 post-smoother that forms z and the CG scalars.  block: threads per block of
-// the 6-RHS level-0 residual (the tuned block of the 6-RHS SpMV, whose access pattern it shares).
+// the 6-RHS level-0 residual and post-smoother (the tuned block of the 6-RHS SpMV, whose access pattern they
+// share).
 void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
   const int L = (int)mg_mesh_.size();
   KernelTimer &fine = (nr == 1) ? t_mg1_ : t_mg6_;
   for (int l = 0; l + 1 < L; ++l) {
     if (l == 0) timer_begin(fine, 0.0);
-    check_launch(mgb_launch_mg_resid(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, block, stream_),
+    check_launch(mgb_launch_mg_resid(&mg_mesh_[l], d_insts_, d_list_, nlist, nr, l, block, mg_half_ ? 1 : 0,
+                                     stream_),
                  "multigrid residual");
     if (l == 0) {
       timer_end(fine);
@@ -999,7 +1060,8 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
   }
   timer_end(t_mgc_);
   timer_begin(fine, 0.0);
-  check_launch(mgb_launch_mg_post0(&mesh_, d_insts_, d_list_, nlist, nr, 1.0f, setup ? 1 : 0, stream_),
+  check_launch(mgb_launch_mg_post0(&mesh_, d_insts_, d_list_, nlist, nr, 1.0f, setup ? 1 : 0, block, mg_half_ ? 1 : 0,
+                                   stream_),
                "multigrid level-0 post-smoother");
   timer_end(fine);
   launches_ += 2 * (L - 1) + 2 * kMgCoarsePairs + (L - 1) + (L - 2) + 1;
@@ -1011,6 +1073,10 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
 std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_mg) {
   const int n = (int)slots.size();
   const bool mg = mg_ && use_mg;
+  // The gather assembly (elastic and damage phases) gives a symmetric tangent: ctan in the energy form.
+  const bool energy = gather32_;
+  const double sweep_rel = energy ? kTangentSweepRelEnergy : kTangentSweepRel;
+  const double tangent_tol = energy ? kTangentTolEnergy : kTangentTol;
   std::vector<char> mg_capped(n, 0);  // a multigrid sweep of the slot reached kMgMaxIts
   std::vector<int> its(n, 0);
   upload_insts();
@@ -1031,7 +1097,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
     for (int s : live) {
       Cg6State c{};
       c.min_err = 0.0;
-      c.rel_err = kTangentSweepRel;
+      c.rel_err = sweep_rel;
       c.max_its = mg ? std::min(cg_max_its_, kMgMaxIts) : cg_max_its_;
       check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
     }
@@ -1045,7 +1111,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
     for (size_t a = 0; a < live.size(); ++a) {
       const InstOut &o = h_out_[live[a]];
       bool ok = true;
-      for (int r = 0; r < 6; ++r) ok &= o.res6[r] <= kTangentTol * o.f6[r];
+      for (int r = 0; r < 6; ++r) ok &= o.res6[r] <= tangent_tol * o.f6[r];
       if (!ok && std::isfinite(o.res6[0])) {
         next.push_back(live[a]);
         next_idx.push_back(live_idx[a]);
@@ -1060,7 +1126,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
       for (int s : live) {
         Cg6State c{};
         c.min_err = 0.0;
-        c.rel_err = kTangentSweepRel;
+        c.rel_err = sweep_rel;
         c.max_its = mg ? std::min(cg_max_its_, kMgMaxIts) : cg_max_its_;
         check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
       }
@@ -1110,10 +1176,24 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
       }
     }
   }
+  if (energy) {
+    // The energy form's interior term needs the refinement residual of the final corrections: slots that left
+    // the loop at the sweep cap get theirs now (the others' is in R6 from their last check).
+    if (!live.empty()) {
+      upload_list(live);
+      launches_ += 1;
+      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), 0, mg ? 1 : 0, stream_),
+                   "tangent residual");
+    }
+    upload_list(slots);
+    launches_ += 1;
+    check_launch(mgb_launch_t6_ecorr(&mesh_, d_insts_, d_list_, n, stream_), "ctan energy term");
+  }
   upload_list(slots);
   launches_ += 1;
   if (gather32_)
-    check_launch(mgb_launch_ctan_react(&mesh_, d_bnodes_, nbnodes_, d_insts_, d_list_, n, stream_), "ctan reactions");
+    check_launch(mgb_launch_ctan_react(&mesh_, d_bnodes_, nbnodes_, d_insts_, d_list_, n, energy ? 1 : 0, stream_),
+                 "ctan reactions");
   else
     check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
   download_out();
@@ -1132,6 +1212,106 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
     }
   }
   return its;
+}
+
+// One Newton iteration of the mixed form with the multigrid for the nlist slots listed in d_list_, as one CUDA
+// graph: the FP32 assembly with the multigrid operators, the CG start (tolerances from d_eta_), a WHILE node
+// whose body runs a chunk of preconditioned CG iterations and then a kernel that continues the loop while some
+// listed instance still iterates (at most min(cg_max_its, kMgMaxIts) / kMgChunk + 2 chunks), u += du and the
+// FP64 residual.  The host's part of an iteration -- the tolerances before it, convergence, the line search and
+// the Jacobi redo of a capped solve after it -- stays outside.  A graph is built the first time a batch size
+// runs once the SpMV autotuner has picked that batch size's block (the autotuner times live launches, which a
+// capture cannot hold) and is replayed afterwards: its kernels read the listed instances and the tolerances
+// from device memory.
+bool Engine::newton_graph(int nlist) {
+  if (!newton_graphs_ok_ || known_block(0, nlist) == 0) return false;
+  auto it = newton_graphs_.find(nlist);
+  if (it == newton_graphs_.end()) {
+    const int block = known_block(0, nlist);
+    const int chunk = kMgChunk;
+    const int max_its = std::min(cg_max_its_, kMgMaxIts);
+    const unsigned cap = (unsigned)(max_its / chunk + 2);
+    const std::vector<int> listed(nlist);  // residual() takes the count of the listed slots only
+    auto capture = [&](cudaGraph_t into, const std::function<void()> &body) {
+      if (into)
+        check(cudaStreamBeginCaptureToGraph(stream_, into, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+              "graph capture");
+      else
+        check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
+      cudaGraph_t out = nullptr;
+      try {
+        body();
+      } catch (...) {
+        cudaStreamEndCapture(stream_, &out);
+        if (out && !into) cudaGraphDestroy(out);
+        throw;
+      }
+      check(cudaStreamEndCapture(stream_, &out), "graph capture end");
+      return out;
+    };
+    NewtonGraph ng;
+    const long l0 = launches_;
+    cudaGraph_t g = nullptr, prefix = nullptr, suffix = nullptr;
+    try {
+      prefix = capture(nullptr, [&] {
+        assemble32(nlist);
+        check_launch(mgb_launch_cg32_init(d_insts_, d_list_, nlist, d_eta_, cg_abs_tol_, max_its, stream_),
+                     "cg32 init");
+        check_launch(mgb_launch_zero_u32(d_chunks_, stream_), "chunk count");
+        check_launch(mgb_launch_cg32_setup(&mesh_, d_insts_, d_list_, nlist, 1, stream_), "cg32 setup");
+        mg_vcycle(1, nlist, true, 128);
+      });
+      launches_ += 3;
+      suffix = capture(nullptr, [&] {
+        check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, nlist, stream_), "u += du");
+        residual(listed);
+      });
+      launches_ += 1;
+      ng.fixed_launches = launches_ - l0;
+      check(cudaGraphCreate(&g, 0), "graph");
+      cudaGraphNode_t n1 = nullptr, n2 = nullptr, n3 = nullptr;
+      check(cudaGraphAddChildGraphNode(&n1, g, nullptr, 0, prefix), "graph prefix");
+      cudaGraphConditionalHandle cond;
+      check(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault), "graph condition");
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = cond;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      check(cudaGraphAddNode(&n2, g, &n1, nullptr, 1, &cp), "graph loop");
+      const long l1 = launches_;
+      capture(cp.conditional.phGraph_out[0], [&] {
+        for (int k = 0; k < chunk; ++k) {
+          if (k == chunk - 1) check_launch(mgb_launch_zero_u32(d_count_, stream_), "count reset");
+          check_launch(mgb_launch_cg32_spmv(&mesh_, d_insts_, d_list_, nlist, block, stream_), "cg32 spmv");
+          check_launch(mgb_launch_cg32_update(&mesh_, d_insts_, d_list_, nlist, 1, stream_), "cg32 update");
+          mg_vcycle(1, nlist, false, 128);
+          check_launch(mgb_launch_cg32_pupdate(&mesh_, d_insts_, d_list_, nlist, d_count_, stream_),
+                       "cg32 p-update");
+        }
+        check_launch(mgb_launch_cg_continue(cond, d_count_, d_chunks_, cap, stream_), "cg loop condition");
+      });
+      ng.chunk_launches = (launches_ - l1) + 3 * chunk + 2;
+      check(cudaGraphAddChildGraphNode(&n3, g, &n2, 1, suffix), "graph suffix");
+      check(cudaGraphInstantiate(&ng.exec, g, 0), "graph instantiate");
+    } catch (const std::exception &) {
+      // Graphs of this form are unavailable here (for instance no conditional nodes): run unfused from now on.
+      for (cudaGraph_t x : {g, prefix, suffix})
+        if (x) cudaGraphDestroy(x);
+      cudaGetLastError();
+      launches_ = l0;
+      newton_graphs_ok_ = false;
+      return false;
+    }
+    for (cudaGraph_t x : {g, prefix, suffix}) cudaGraphDestroy(x);
+    launches_ = l0;
+    it = newton_graphs_.emplace(nlist, ng).first;
+  }
+  check(cudaGraphLaunch(it->second.exec, stream_), "graph launch");
+  check(cudaMemcpyAsync(h_chunks_, d_chunks_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_), "chunks");
+  sync();
+  launches_ += it->second.fixed_launches + (long)*h_chunks_ * it->second.chunk_launches;
+  return true;
 }
 
 // newton_raphson (solve.cpp:28-82) for a batch: slot s solves for strains[i] with its h_insts_ vars_old.
@@ -1192,8 +1372,11 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     bool have_residual = false;
     bool a0_iteration = false;
     std::vector<int> mg_its(na, 0);  // iterations of multigrid solves redone with Jacobi
+    // The mixed multigrid form runs the iteration's device work as one CUDA graph where it can (graphs on,
+    // kernel timers off); otherwise kernel by kernel.
+    const bool fused = mixed && mg_ && graphs_ && !timing_on() && newton_graphs_ok_ && known_block(0, na) > 0;
     if (mixed) {
-      assemble32(na);
+      if (!fused) assemble32(na);
     } else if (use_A0_ && !exact_tangent_ && res[idx[0]].its < its_with_A0_) {
       // solve.cpp:55-66: this iteration solves with A0 (every active slot started this Newton together, so
       // they share the iteration count)
@@ -1223,9 +1406,16 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
         const double want = (norm[i] > 0) ? 0.05 * nr_rel_tol_ * norm0[i] / norm[i] : floor;
         eta[a] = std::max(floor, std::min(0.1, want));
       }
-      cg_solve32(active, eta);
-      if (mg_) {
-        // A multigrid solve that reached its iteration cap is redone from du = 0 with Jacobi.
+      bool graphed = false;
+      if (fused) {
+        for (int a = 0; a < na; ++a) h_eta_[a] = eta[a];
+        check(cudaMemcpyAsync(d_eta_, h_eta_, na * sizeof(double), cudaMemcpyHostToDevice, stream_), "CG tolerances");
+        graphed = newton_graph(na);
+        if (!graphed) assemble32(na);  // the graph could not be built: the unfused iteration follows
+      }
+      if (graphed) {
+        // assembly, solve, u += du and the residual have run; a multigrid solve that reached its cap is undone
+        // and redone from du = 0 with Jacobi, then the residual of those slots is taken again
         download_out();
         std::vector<int> redo;
         std::vector<double> redo_eta;
@@ -1236,15 +1426,42 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
             redo_eta.push_back(eta[a]);
           }
         if (!redo.empty()) {
+          for (int s : redo) {
+            launches_ += 1;
+            check_launch(mgb_launch_axpy_du32(&mesh_, slots_[s].u, slots_[s].du32, -1.0, stream_), "undo du");
+          }
           upload_list(redo);
           cg_solve32(redo, redo_eta, false);
+          launches_ += 1;
+          check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, (int)redo.size(), stream_), "u += du");
+          residual(redo);
           upload_list(active);
+          download_out();
         }
+      } else {
+        cg_solve32(active, eta);
+        if (mg_) {
+          // A multigrid solve that reached its iteration cap is redone from du = 0 with Jacobi.
+          download_out();
+          std::vector<int> redo;
+          std::vector<double> redo_eta;
+          for (int a = 0; a < na; ++a)
+            if (h_out_[active[a]].cg_maxed) {
+              mg_its[a] = h_out_[active[a]].cg_its;
+              redo.push_back(active[a]);
+              redo_eta.push_back(eta[a]);
+            }
+          if (!redo.empty()) {
+            upload_list(redo);
+            cg_solve32(redo, redo_eta, false);
+            upload_list(active);
+          }
+        }
+        launches_ += 1;
+        check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
+        residual(active);
+        download_out();
       }
-      launches_ += 1;
-      check_launch(mgb_launch_add_du32(&mesh_, d_insts_, d_list_, na, stream_), "u += du");
-      residual(active);
-      download_out();
       have_residual = true;
       // Backtracking line search per instance (Armijo on |b|, step halved up to 8 times): a full step that
       // does not reduce the residual (J2 points crossing the yield surface) is shortened.

@@ -48,6 +48,7 @@ struct Slot {
   float *gpd = nullptr;
   MgInst *mg = nullptr;          // device copy of the multigrid hierarchy's pointers
   std::vector<float *> mg_bufs;  // its buffers
+  std::vector<unsigned short *> mg_bufs16;
   unsigned int *ticket = nullptr;
   CgState *cg = nullptr;
   Cg6State *cg6 = nullptr;
@@ -184,7 +185,13 @@ class Engine {
   void run_chunk(int kind, int n, const std::function<void()> &body);
   // Block size of the FP32 SpMV (kind 0) or the 6-RHS SpMV (kind 1) for this RVE size and batch (autotuned).
   int tuned_block(int kind, int nlist);
+  // The tuned block if the autotuner has already run for (kind, RVE size, nlist), else 0.
+  int known_block(int kind, int nlist) const;
   void clear_graphs();
+  bool timing_on() const;
+  // One Newton iteration of the mixed multigrid form for the nlist slots in d_list_ (tolerances in d_eta_) as
+  // one CUDA graph with a WHILE node over the CG chunks; false where graphs cannot be used (then nothing ran).
+  bool newton_graph(int nlist);
   int bicg_solve(bool transpose, double *x);
   // Multigrid (engine.cpp): Galerkin operators of the listed slots after an FP32 assembly; one V-cycle of the
   // 1- or 6-RHS CG of the listed slots, ending with the level-0 post-smoother (setup: start of a solve).
@@ -214,6 +221,8 @@ class Engine {
   int nsubiterations_ = 10;
   int precision_ = 0, ctan_mode_ = 0;
   bool mg_ = false;                 // the FP32 solves are multigrid-preconditioned
+  bool mg_half_ = false;            // ... with the FP16 copy of the fine operator in the level-0 smoothing passes
+  float mg_scale16_ = 1.0f;         // power-of-two scale of that copy
   std::vector<MeshDev> mg_mesh_;    // grids of the multigrid levels (level 0 = mesh_)
   bool exact_tangent_ = false;  // FP64 Newton with the exact tangent and BiCGSTAB corrections (paths, slot 0)
   bool use_A0_ = false;         // micropp.cpp:128-143: the first its_with_A0 FP64 Newton iterations solve with A0
@@ -257,6 +266,17 @@ class Engine {
   PathState path_;
   bool graphs_ = true;                         // CG chunks replayed from captured CUDA graphs
   std::map<long, cudaGraphExec_t> graph_cache_;  // (solver, listed instances) -> executable graph
+  // Newton-iteration graphs of the mixed multigrid form, per number of listed instances.
+  struct NewtonGraph {
+    cudaGraphExec_t exec = nullptr;
+    long fixed_launches = 0;  // kernels outside the WHILE node
+    long chunk_launches = 0;  // kernels per pass of its body
+  };
+  std::map<int, NewtonGraph> newton_graphs_;
+  bool newton_graphs_ok_ = true;               // cleared if building one fails (the iteration then runs unfused)
+  double *d_eta_ = nullptr, *h_eta_ = nullptr;  // CG tolerances of the listed slots (device, pinned host)
+  int eta_cap_ = 0;
+  unsigned int *d_chunks_ = nullptr, *h_chunks_ = nullptr;  // chunks the last captured CG loop ran
 };
 
 }  // namespace mgb

@@ -56,6 +56,14 @@ int mgb_launch_cg32_update(const mgb::MeshDev *m, const mgb::Inst *insts, const 
 int mgb_launch_cg32_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                             unsigned int *active_count, cudaStream_t s);
 int mgb_launch_add_du32(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// CG states of the listed instances at the start of a solve, from a device array of relative tolerances.
+int mgb_launch_cg32_init(const mgb::Inst *insts, const int *list, int nlist, const double *rel_tol, double abs_tol,
+                         int max_its, cudaStream_t s);
+// *p = 0 (a kernel, so that it can sit in a conditional node's body).
+int mgb_launch_zero_u32(unsigned int *p, cudaStream_t s);
+// The condition of a captured CG loop (a WHILE node): continue while *count != 0 and fewer than cap chunks ran.
+int mgb_launch_cg_continue(cudaGraphConditionalHandle h, const unsigned int *count, unsigned int *chunks,
+                           unsigned int cap, cudaStream_t s);
 int mgb_launch_axpy_du32(const mgb::MeshDev *m, double *u, const float *du, double a, cudaStream_t s);
 int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
@@ -70,8 +78,11 @@ int mgb_launch_t6_accumulate(const mgb::MeshDev *m, const mgb::Inst *insts, cons
                              cudaStream_t s);
 // ctan from the boundary reactions of the tangent fields (gather-assembled FP32 Jacobian); bnodes lists the nbn
 // boundary nodes.
+// energy = 1: the energy form (symmetric tangents), with the interior term of mgb_launch_t6_ecorr.
 int mgb_launch_ctan_react(const mgb::MeshDev *m, const int *bnodes, int nbn, const mgb::Inst *insts, const int *list,
-                          int nlist, cudaStream_t s);
+                          int nlist, int energy, cudaStream_t s);
+// Interior term of the energy form of ctan from X6 and the last refinement residual in R6.
+int mgb_launch_t6_ecorr(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 
@@ -85,17 +96,21 @@ int mgb_launch_mg_rap1(const mgb::MeshDev *mi, const mgb::MeshDev *mo, const mgb
 // Inverse safeguarded smoother diagonal of level l: 1 / max(a_dd / omega, c sum_j |a_dj|).
 int mgb_launch_mg_sdiag(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int l,
                         float omega, float c, cudaStream_t s);
-// block: threads per block of the 6-RHS level-0 residual (64, 128 or 256; two nodes per thread).
+// block: threads per block of the 6-RHS level-0 residual (64, 128 or 256; two nodes per thread).  half: the
+// level-0 passes read the FP16 copy of the fine operator (MgInst::vals16).
 int mgb_launch_mg_resid(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
-                        int block, cudaStream_t s);
+                        int block, int half, cudaStream_t s);
+// The FP16 copy of the level-0 operator, scale16 x vals32, of the listed instances.
+int mgb_launch_mg_half0(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_mg_restrict(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,
                            int nlist, int nr, int lf, float omega, cudaStream_t s);
 int mgb_launch_mg_prolong(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const mgb::Inst *insts, const int *list,
                           int nlist, int nr, int lf, cudaStream_t s);
 int mgb_launch_mg_jacobi(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
                          int src, int dst, float omega, cudaStream_t s);
+// block: threads per block of the 6-RHS form (64, 128 or 256; two nodes per thread), as mgb_launch_mg_resid.
 int mgb_launch_mg_post0(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr,
-                        float omega, int setup, cudaStream_t s);
+                        float omega, int setup, int block, int half, cudaStream_t s);
 
 // Adjoint of a load path (adjoint_kernels.cu); one instance (list[0]).
 int mgb_launch_node_gather(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);

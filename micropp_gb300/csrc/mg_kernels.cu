@@ -30,6 +30,10 @@
 // for six; the level-0 residual and prolongation go to lv[0].t (3 * nn or 18 * np floats).  Every kernel
 // writes zeros on boundary nodes, so coarse vectors never carry values there.  Launch order on one stream is
 // the only synchronisation; reductions use the last-block ticket of reduce.cuh.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
 #include "device.cuh"
 #include "launch.h"
 #include "reduce.cuh"
@@ -38,6 +42,19 @@ namespace mgb {
 namespace {
 
 constexpr int kMgBlock = 128;
+
+// The FP16 copy of the level-0 operator (MICROPP3_PRECOND_MG_HALF): scale16 x the FP32 values, streamed by the
+// two level-0 smoothing passes; their sums are rescaled by inv16, an exact power of two.
+__device__ __forceinline__ float ld_h(const unsigned short *__restrict__ p) {
+  return __half2float(__ushort_as_half(__ldcs(p)));
+}
+
+// Two consecutive FP16 entries (nodes n0, n0 + 1) in one 4-byte load.
+__device__ __forceinline__ float2 ld_h2(const unsigned int *__restrict__ p) {
+  const unsigned int b = __ldcs(p);
+  return __half22float2(__halves2half2(__ushort_as_half((unsigned short)(b & 0xffffu)),
+                                       __ushort_as_half((unsigned short)(b >> 16))));
+}
 
 // Index of component (r, d) of node n in a level's vector: node-interleaved for a single right-hand side on
 // level 0 (RM), component-major otherwise.
@@ -117,6 +134,34 @@ __device__ __forceinline__ void apply_node(const MeshDev &m, const float *__rest
         for (int fj = 0; fj < 3; ++fj) y[r * 3 + fi] = fmaf(K[fi * 3 + fj], xv[fj], y[r * 3 + fi]);
     }
   }
+}
+
+// apply_node on level 0 with the FP16 copy of the operator (streamed), rescaled once.
+template <int NR, bool RM>
+__device__ __forceinline__ void apply_node_h(const MeshDev &m, const unsigned short *__restrict__ vals, float inv,
+                                             const float *__restrict__ x, int n, float (&y)[NR * 3]) {
+  const size_t np = m.np;
+#pragma unroll
+  for (int c = 0; c < NR * 3; ++c) y[c] = 0.f;
+#pragma unroll 3
+  for (int s = 0; s < 27; ++s) {
+    const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
+    float K[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) K[q] = ld_h(vals + (size_t)(s * 9 + q) * np + n);
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      float xv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xv[d] = x[vix<RM>(r, d, nb, np)];
+#pragma unroll
+      for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj) y[r * 3 + fi] = fmaf(K[fi * 3 + fj], xv[fj], y[r * 3 + fi]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NR * 3; ++c) y[c] *= inv;
 }
 
 // One 1-D step of the separable Galerkin product: P = Px Py Pz (each a 1-D interpolation with the Dirichlet
@@ -215,8 +260,8 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_sdiag(MeshDev m, const Inst *in
   }
 }
 
-// t_l = b_l - A_l x_l (zero on boundary nodes).
-template <int NR, bool RM, bool STREAM>
+// t_l = b_l - A_l x_l (zero on boundary nodes); HALF (level 0): A from the FP16 copy.
+template <int NR, bool RM, bool STREAM, bool HALF = false>
 __global__ void __launch_bounds__(kMgBlock) k_mg_resid(MeshDev m, const Inst *insts, const int *list, int l) {
   const Inst &I = insts[list[blockIdx.y]];
   if (inst_done<NR>(I)) return;
@@ -233,7 +278,10 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_resid(MeshDev m, const Inst *in
     return;
   }
   float y[NR * 3];
-  apply_node<NR, RM, STREAM>(m, v.vals, v.x, n, y);
+  if constexpr (HALF)
+    apply_node_h<NR, RM>(m, I.mg->vals16, I.mg->inv16, v.x, n, y);
+  else
+    apply_node<NR, RM, STREAM>(m, v.vals, v.x, n, y);
 #pragma unroll
   for (int r = 0; r < NR; ++r)
 #pragma unroll
@@ -390,7 +438,7 @@ __device__ __forceinline__ void post0_scalars(const Inst &I, const double (&tot)
 
 // Level-0 post-smoother and the CG scalars: z = t0 + w D^-1 (r - A t0), rz_i = sum r.z.  setup: p = z and
 // rz = rz_i (start of a solve); otherwise beta = rz_i / rz, rz = rz_i (right-hand sides still iterating).
-template <int NR, bool RM>
+template <int NR, bool RM, bool HALF = false>
 __global__ void __launch_bounds__(kMgBlock) k_mg_post0(MeshDev m, const Inst *insts, const int *list, float omega,
                                                        int setup) {
   const Inst &I = insts[list[blockIdx.y]];
@@ -406,7 +454,12 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_post0(MeshDev m, const Inst *in
     int i, j, k;
     const bool bn = on_boundary(m, n, i, j, k);
     float y[NR * 3];
-    if (!bn) apply_node<NR, RM, true>(m, v.vals, v.t, n, y);
+    if (!bn) {
+      if constexpr (HALF)
+        apply_node_h<NR, RM>(m, I.mg->vals16, I.mg->inv16, v.t, n, y);
+      else
+        apply_node<NR, RM, true>(m, v.vals, v.t, n, y);
+    }
 #pragma unroll
     for (int r = 0; r < NR; ++r)
 #pragma unroll
@@ -428,10 +481,13 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_post0(MeshDev m, const Inst *in
 // of a pair row along x loaded once for the 3 x-slots, neighbour indices clamped into the grid (the sums of
 // boundary nodes are discarded).  Same products and order per row as apply_node.  Held to 128 registers (512
 // threads per SM), the residency of the tangent CG's SpMV.
+template <bool HALF>
 __device__ __forceinline__ void apply_pair6(const MeshDev &m, const float *__restrict__ vals,
+                                            const unsigned short *__restrict__ vals16, float inv,
                                             const float *__restrict__ x, int n0, float (&y)[2][18]) {
   const size_t np = m.np, np2 = np / 2;
   const float2 *__restrict__ v2 = reinterpret_cast<const float2 *>(vals + n0);
+  const unsigned int *__restrict__ h2 = reinterpret_cast<const unsigned int *>(vals16 + n0);
   const int last = m.nn - 1;
 #pragma unroll
   for (int q = 0; q < 2; ++q)
@@ -447,7 +503,13 @@ __device__ __forceinline__ void apply_pair6(const MeshDev &m, const float *__res
 #pragma unroll
     for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-      for (int e = 0; e < 9; ++e) a[dx][e] = __ldcs(v2 + (size_t)((zy * 3 + dx) * 9 + e) * np2);
+      for (int e = 0; e < 9; ++e) {
+        const size_t o = (size_t)((zy * 3 + dx) * 9 + e) * np2;
+        if constexpr (HALF)
+          a[dx][e] = ld_h2(h2 + o);
+        else
+          a[dx][e] = __ldcs(v2 + o);
+      }
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
       float xv[4][3];
@@ -465,10 +527,16 @@ __device__ __forceinline__ void apply_pair6(const MeshDev &m, const float *__res
         }
     }
   }
+  if constexpr (HALF) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int c = 0; c < 18; ++c) y[q][c] *= inv;
+  }
 }
 
 // t0 = r - A x0 for the 6 right-hand sides (zero on boundary nodes), two nodes per thread.
-template <int B>
+template <int B, bool HALF>
 __global__ void __launch_bounds__(B, 512 / B) k_mg_resid6(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg6->all_done) return;
@@ -483,7 +551,7 @@ __global__ void __launch_bounds__(B, 512 / B) k_mg_resid6(MeshDev m, const Inst 
     bn[q] = (n0 + q >= m.nn) || on_boundary(m, n0 + q, i, j, k);
   }
   float y[2][18];
-  if (!bn[0] || !bn[1]) apply_pair6(m, v.vals, v.x, n0, y);
+  if (!bn[0] || !bn[1]) apply_pair6<HALF>(m, v.vals, I.mg->vals16, I.mg->inv16, v.x, n0, y);
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
     const int n = n0 + q;
@@ -496,7 +564,96 @@ __global__ void __launch_bounds__(B, 512 / B) k_mg_resid6(MeshDev m, const Inst 
   }
 }
 
+// Level-0 post-smoother of the 6-RHS V-cycle with the pair structure of k_mg_resid6: z = t0 + w D^-1 (r - A t0)
+// and rz_i = sum r.z for two consecutive nodes per thread; setup: p = z.  The CG scalars as in k_mg_post0.
+// Bounded to 384 threads per SM (about 168 registers): at 128 registers it spills.
+template <int B, bool HALF>
+__global__ void __launch_bounds__(B, 384 / B) k_mg_post06(MeshDev m, const Inst *insts, const int *list,
+                                                          float omega, int setup) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (I.cg6->all_done) return;
+  const int n0 = (blockIdx.x * B + threadIdx.x) * 2;
+  float acc[6];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) acc[r] = 0.f;
+  if (n0 < m.nn) {
+    const LvView v = view<6>(I, 0);
+    float *__restrict__ p = I.P6;
+    const size_t np = m.np;
+    bool bn[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      int i, j, k;
+      bn[q] = (n0 + q >= m.nn) || on_boundary(m, n0 + q, i, j, k);
+    }
+    float y[2][18];
+    if (!bn[0] || !bn[1]) apply_pair6<HALF>(m, v.vals, I.mg->vals16, I.mg->inv16, v.t, n0, y);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int n = n0 + q;
+      if (n >= m.nn) break;
+      float kd[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) kd[d] = omega * v.kinv[(size_t)n * 3 + d];
+#pragma unroll
+      for (int c = 0; c < 18; ++c) {
+        const size_t idx = (size_t)c * np + n;
+        const float rv = v.b[idx];
+        const float z = bn[q] ? 0.f : fmaf(kd[c % 3], rv - y[q][c], v.t[idx]);
+        v.x[idx] = z;
+        if (setup) p[idx] = z;
+        acc[c / 3] = fmaf(rv, z, acc[c / 3]);
+      }
+    }
+  }
+  double tot[6];
+  if (grid_sum_f<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) post0_scalars<6>(I, tot, setup);
+}
+
+// The FP16 copy of the level-0 operator: vals16 = fp16(scale16 x vals32), four entries per thread and step
+// (243 np entries, np a multiple of 32), clamped to the FP16 range.
+__global__ void __launch_bounds__(256) k_mg_half0(MeshDev m, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const MgInst &G = *I.mg;
+  const size_t count4 = (size_t)kEllPerNode * m.np / 4;
+  const float s = G.scale16;
+  const float4 *__restrict__ src = reinterpret_cast<const float4 *>(I.vals32);
+  uint2 *__restrict__ dst = reinterpret_cast<uint2 *>(G.vals16);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count4; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 v = __ldcs(src + i);
+    const float c[4] = {v.x, v.y, v.z, v.w};
+    unsigned short h[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_rn(fminf(fmaxf(c[k] * s, -65504.f), 65504.f)));
+    dst[i] = make_uint2((unsigned)h[0] | ((unsigned)h[1] << 16), (unsigned)h[2] | ((unsigned)h[3] << 16));
+  }
+}
+
 inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+template <bool HALF>
+void launch_resid6(const MeshDev *m, const Inst *insts, const int *list, int nlist, int block, cudaStream_t s) {
+  const size_t pairs = cdiv(m->nn, 2);
+  if (block == 64)
+    k_mg_resid6<64, HALF><<<dim3(cdiv(pairs, 64), nlist), 64, 0, s>>>(*m, insts, list);
+  else if (block == 256)
+    k_mg_resid6<256, HALF><<<dim3(cdiv(pairs, 256), nlist), 256, 0, s>>>(*m, insts, list);
+  else
+    k_mg_resid6<128, HALF><<<dim3(cdiv(pairs, 128), nlist), 128, 0, s>>>(*m, insts, list);
+}
+
+// two nodes per thread: at most cdiv(nn, 128) blocks, the reduction partials' capacity
+template <bool HALF>
+void launch_post06(const MeshDev *m, const Inst *insts, const int *list, int nlist, float omega, int setup, int block,
+                   cudaStream_t s) {
+  const size_t pairs = cdiv(m->nn, 2);
+  if (block == 64)
+    k_mg_post06<64, HALF><<<dim3(cdiv(pairs, 64), nlist), 64, 0, s>>>(*m, insts, list, omega, setup);
+  else if (block == 256)
+    k_mg_post06<256, HALF><<<dim3(cdiv(pairs, 256), nlist), 256, 0, s>>>(*m, insts, list, omega, setup);
+  else
+    k_mg_post06<128, HALF><<<dim3(cdiv(pairs, 128), nlist), 128, 0, s>>>(*m, insts, list, omega, setup);
+}
 
 }  // namespace
 }  // namespace mgb
@@ -521,22 +678,29 @@ int mgb_launch_mg_sdiag(const MeshDev *m, const Inst *insts, const int *list, in
   return (int)cudaGetLastError();
 }
 
+int mgb_launch_mg_half0(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  const size_t count4 = (size_t)kEllPerNode * m->np / 4;
+  const unsigned blocks = (unsigned)std::min<size_t>(cdiv(count4, 256), 1216);
+  k_mg_half0<<<dim3(blocks, nlist), 256, 0, s>>>(*m, insts, list);
+  return (int)cudaGetLastError();
+}
+
 int mgb_launch_mg_resid(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l, int block,
-                        cudaStream_t s) {
+                        int half, cudaStream_t s) {
   if (nlist <= 0) return 0;
   if (nr == 6 && l == 0) {
-    const size_t pairs = cdiv(m->nn, 2);
-    if (block == 64)
-      k_mg_resid6<64><<<dim3(cdiv(pairs, 64), nlist), 64, 0, s>>>(*m, insts, list);
-    else if (block == 256)
-      k_mg_resid6<256><<<dim3(cdiv(pairs, 256), nlist), 256, 0, s>>>(*m, insts, list);
+    if (half)
+      launch_resid6<true>(m, insts, list, nlist, block, s);
     else
-      k_mg_resid6<128><<<dim3(cdiv(pairs, 128), nlist), 128, 0, s>>>(*m, insts, list);
+      launch_resid6<false>(m, insts, list, nlist, block, s);
     return (int)cudaGetLastError();
   }
   const dim3 g(cdiv(m->nn, kMgBlock), nlist);
   if (nr == 1) {
-    if (l == 0)
+    if (l == 0 && half)
+      k_mg_resid<1, true, true, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
+    else if (l == 0)
       k_mg_resid<1, true, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
     else
       k_mg_resid<1, false, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, l);
@@ -589,13 +753,20 @@ int mgb_launch_mg_jacobi(const MeshDev *m, const Inst *insts, const int *list, i
 }
 
 int mgb_launch_mg_post0(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, float omega,
-                        int setup, cudaStream_t s) {
+                        int setup, int block, int half, cudaStream_t s) {
   if (nlist <= 0) return 0;
+  if (nr == 6) {
+    if (half)
+      launch_post06<true>(m, insts, list, nlist, omega, setup, block, s);
+    else
+      launch_post06<false>(m, insts, list, nlist, omega, setup, block, s);
+    return (int)cudaGetLastError();
+  }
   const dim3 g(cdiv(m->nn, kMgBlock), nlist);
-  if (nr == 1)
-    k_mg_post0<1, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
+  if (half)
+    k_mg_post0<1, true, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
   else
-    k_mg_post0<6, false><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
+    k_mg_post0<1, true><<<g, kMgBlock, 0, s>>>(*m, insts, list, omega, setup);
   return (int)cudaGetLastError();
 }
 

@@ -652,8 +652,12 @@ __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
 // On interior rows f_n = -RF_n, the final refinement residual (below the tangent tolerance), so the sum runs
 // over the boundary nodes; the shear entries take the symmetric part.  One thread per boundary node, FP64
 // accumulation of the FP32 matrix values.
+//
+// energy = 1 (symmetric tangent): ctan[k][i] = (1/V) v_k^T K v_i with v = w + x, the energy form, whose error is
+// quadratic in the error of x where the boundary sum's is linear.  With (K v_i) = -RF_i on interior rows it is
+// the boundary sum minus (1/V) sum over interior nodes of x_k . RF_i (Cg6State::ecorr, k_t6_ecorr).
 __global__ void __launch_bounds__(kNodeBlock) k_ctan_react(MeshDev m, const int *bnodes, int nbn, const Inst *insts,
-                                                           const int *list) {
+                                                           const int *list, int energy) {
   const Inst &I = insts[list[blockIdx.y]];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[36];
@@ -708,11 +712,44 @@ __global__ void __launch_bounds__(kNodeBlock) k_ctan_react(MeshDev m, const int 
   if (grid_sum<36>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     bool bad = false;
     for (int q = 0; q < 36; ++q) {
-      I.out->ctan[q] = tot[q] / m.vol_tot;
-      bad |= !isfinite(tot[q]);
+      const double t = energy ? tot[q] - I.cg6->ecorr[q] : tot[q];
+      I.out->ctan[q] = t / m.vol_tot;
+      bad |= !isfinite(t);
     }
     if (bad) I.out->nonfinite = 1;
   }
+}
+
+// Interior term of the energy form of ctan: ecorr[k * 6 + i] = sum over interior nodes of x_k . RF_i, with x the
+// tangent corrections (X6) and RF_i the refinement residual of the final X6 as k_t6_residual left it in R6 (its
+// FP32 rounding only moves this correction term by ~1e-7 of itself).  One thread per node, FP64 sums.
+__global__ void __launch_bounds__(kNodeBlock) k_t6_ecorr(MeshDev m, const Inst *insts, const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[36];
+#pragma unroll
+  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
+  if (n < m.nn) {
+    int i, j, k;
+    if (!bnd(m, n, i, j, k)) {
+      const size_t np = m.np;
+      double x[6][3], rf[6][3];
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          x[r][d] = I.X6[c6(r, d, np) + n];
+          rf[r][d] = (double)I.R6[c6(r, d, np) + n];
+        }
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) acc[a * 6 + b] = x[a][0] * rf[b][0] + x[a][1] * rf[b][1] + x[a][2] * rf[b][2];
+    }
+  }
+  double tot[36];
+  if (grid_sum<36>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
+    for (int q = 0; q < 36; ++q) I.cg6->ecorr[q] = tot[q];
 }
 
 // ctan[v][i] = (1/V) sum over Gauss points of wg (C_gp B (w_i + x_i))_v, one thread per Gauss point, FP64.
@@ -802,6 +839,32 @@ __global__ void __launch_bounds__(128) k_ctan_avg(MeshDev m, Mats mats, const in
   }
 }
 
+// CG state of the listed instances at the start of a solve (what the host writes before an uncaptured solve):
+// relative tolerance rel_tol[a] for the a-th listed instance, abs_tol, max_its, everything else zero.
+__global__ void k_cg32_init(const Inst *insts, const int *list, int nlist, const double *rel_tol, double abs_tol,
+                            int max_its) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nlist) return;
+  CgState c{};
+  c.min_err = abs_tol;
+  c.rel_err = rel_tol[a];
+  c.max_its = max_its;
+  *insts[list[a]].cg = c;
+}
+
+__global__ void k_zero_u32(unsigned int *p) { *p = 0u; }
+
+// Condition of the WHILE node of a captured CG solve: another chunk of iterations runs while some instance of
+// the batch still iterates (the count of the chunk's last p-update) and fewer than `cap` chunks have run.  The
+// CG kernels stop every instance at its max_its, so the count reaches zero by itself; the cap bounds the loop
+// all the same.
+__global__ void k_cg_continue(cudaGraphConditionalHandle h, const unsigned int *count, unsigned int *chunks,
+                              unsigned int cap) {
+  const unsigned int c = *chunks + 1u;
+  *chunks = c;
+  cudaGraphSetConditional(h, (*count != 0u && c < cap) ? 1u : 0u);
+}
+
 }  // namespace mgb
 
 using namespace mgb;
@@ -809,6 +872,24 @@ using namespace mgb;
 static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
 extern "C" {
+
+int mgb_launch_cg32_init(const Inst *insts, const int *list, int nlist, const double *rel_tol, double abs_tol,
+                         int max_its, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_cg32_init<<<cdiv(nlist, 128), 128, 0, s>>>(insts, list, nlist, rel_tol, abs_tol, max_its);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_zero_u32(unsigned int *p, cudaStream_t s) {
+  k_zero_u32<<<1, 1, 0, s>>>(p);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_cg_continue(cudaGraphConditionalHandle h, const unsigned int *count, unsigned int *chunks,
+                           unsigned int cap, cudaStream_t s) {
+  k_cg_continue<<<1, 1, 0, s>>>(h, count, chunks, cap);
+  return (int)cudaGetLastError();
+}
 
 int mgb_launch_cg32_setup(const MeshDev *m, const Inst *insts, const int *list, int nlist, int mg, cudaStream_t s) {
   if (nlist <= 0) return 0;
@@ -902,9 +983,15 @@ int mgb_launch_t6_accumulate(const MeshDev *m, const Inst *insts, const int *lis
 }
 
 int mgb_launch_ctan_react(const MeshDev *m, const int *bnodes, int nbn, const Inst *insts, const int *list, int nlist,
-                          cudaStream_t s) {
+                          int energy, cudaStream_t s) {
   if (nlist <= 0 || nbn <= 0) return 0;
-  k_ctan_react<<<dim3(cdiv(nbn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, bnodes, nbn, insts, list);
+  k_ctan_react<<<dim3(cdiv(nbn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, bnodes, nbn, insts, list, energy);
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_t6_ecorr(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return 0;
+  k_t6_ecorr<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
   return (int)cudaGetLastError();
 }
 

@@ -78,6 +78,16 @@ def test_damage_layers_mg_against_jacobi(gpu_lib):
     assert its_mg < 0.6 * its_j, (its_mg, its_j)
 
 
+def test_fp16_smoothing_operator_meets_the_bars(gpu_lib):
+    """MICROPP3_PRECOND_MG_HALF (the level-0 smoothing passes read an FP16 copy of the fine operator): the same
+    bars against the tight oracle, with CG iterations close to the FP32 V-cycle's."""
+    import micropp_gb300 as mg
+    its_h, g = _fast_path(12, damage_kw(12), DAMAGE_PATH, mg.PRECOND_MG_HALF)
+    assert g.mg_levels() == 3
+    its_f, _ = _fast_path(12, damage_kw(12), DAMAGE_PATH, mg.PRECOND_MG)
+    assert its_h <= 1.25 * its_f + 2, (its_h, its_f)
+
+
 @pytest.mark.parametrize("n", [9, (13, 6, 9)])
 def test_odd_and_noncubic_grids(gpu_lib, n):
     import micropp_gb300 as mg
@@ -100,13 +110,14 @@ def test_linear_ctan_mg(gpu_lib):
     assert rel_err(g.ctan_lin(), j.ctan_lin()) < 1e-7
 
 
-def test_batched_mg_uneven_points(gpu_lib):
+@pytest.mark.parametrize("precond", [1, 2], ids=["fp32", "fp16_smoothing"])
+def test_batched_mg_uneven_points(gpu_lib, precond):
     """Four points of one handle, different strains (one stays linear), multigrid batch of uneven solves."""
     import micropp_gb300 as mg
     n = 10
     kw = damage_kw(n)
     kw["coupling"] = [2] * 4
-    g = mg.Micropp(gpu_config(n, ngp=4, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=mg.PRECOND_MG,
+    g = mg.Micropp(gpu_config(n, ngp=4, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=precond,
                               **kw, **FAST))
     o = orc.OracleRVE(oracle_config(n, ngp=4, **kw, **TIGHT))
     assert g.mg_levels() == 3
@@ -123,12 +134,45 @@ def test_batched_mg_uneven_points(gpu_lib):
             assert rel_err(g.get_ctan(gp), o.get_ctan(gp)) < 1e-4
 
 
-def test_damage_path_20_converges_with_mg(gpu_lib):
+@pytest.mark.parametrize("precond", [1, 2], ids=["fp32", "fp16_smoothing"])
+def test_damage_path_20_converges_with_mg(gpu_lib, precond):
     """The 20^3 layered damage step whose first Jacobian (uniform strain (1e-2, -3e-3, 0, 5e-3, 0, 0), loading
     with q/r = 1.67) is strongly anisotropic: lambda_max(D^-1 A) = 4.15 > 2 / 0.6, where a plain damped-Jacobi
     V-cycle stops being positive definite and its CG stalled at the iteration cap in every Newton iteration.
     With the safeguarded smoother diagonal it converges; the results meet the parity bars."""
     import micropp_gb300 as mg
-    its_mg, g = _fast_path(20, damage_kw(20), DAMAGE_PATH, mg.PRECOND_MG)
+    its_mg, g = _fast_path(20, damage_kw(20), DAMAGE_PATH, precond)
     its_j, _ = _fast_path(20, damage_kw(20), DAMAGE_PATH, mg.PRECOND_JACOBI)
     assert its_mg < its_j, (its_mg, its_j)
+
+
+def test_newton_iteration_graphs_match_unfused(gpu_lib):
+    """With CUDA graphs on and kernel timers off, a Newton iteration of the mixed multigrid form runs as one
+    graph (assembly, CG start, a WHILE node over the CG chunks, u += du, residual).  Its kernels and their order
+    are those of the unfused iteration, so stress, ctan and the iteration counts are bitwise the same."""
+    import micropp_gb300 as mg
+    n = 12
+    kw = damage_kw(n)
+    kw["coupling"] = [2] * 3
+    handles = []
+    for graphs in (True, False):
+        g = mg.Micropp(gpu_config(n, ngp=3, precision=mg.MIXED, ctan_mode=mg.CTAN_IMPLICIT, precond=mg.PRECOND_MG,
+                                  **kw, **FAST))
+        g.set_kernel_timing(False)
+        g.set_cuda_graphs(graphs)
+        handles.append(g)
+    strains = [DAMAGE_PATH[1], 0.5 * DAMAGE_PATH[1], -DAMAGE_PATH[0]]
+    for step in range(3):
+        for g in handles:
+            for gp, e in enumerate(strains):
+                g.set_strain(gp, e * (1 + 0.2 * step))
+            g.homogenize()
+        a, b = handles
+        for gp in range(3):
+            assert np.array_equal(a.get_stress(gp), b.get_stress(gp)), (step, gp)
+            assert np.array_equal(a.get_ctan(gp), b.get_ctan(gp)), (step, gp)
+            assert a.newton(gp) == b.newton(gp)
+            assert a.status(gp) == b.status(gp) == mg.STATUS_OK
+        for g in handles:
+            g.update_vars()
+    assert handles[0].total_cg_its() == handles[1].total_cg_its()
