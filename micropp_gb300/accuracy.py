@@ -1,21 +1,24 @@
 """Error of the fast form against a tightly converged FP64 solution, measured with the library itself.
 
-The FP64 solution is the plain form (the reference algorithm in FP64: Newton with the forward-difference
-law tangent and Jacobi-preconditioned CG, homogenize.cpp:188-282, solve.cpp:28-82, ell.cpp:66-122) run far
-below the reference's tolerances: CG to 1e-12 and Newton to 1e-11 of their initial residuals, with the
-absolute Newton stop switched off.  Its ctan is a central difference of that stress,
-ctan[:, j] = (sigma(eps + h e_j) - sigma(eps - h e_j)) / 2h with h = 1e-7.  The thirteen solves (eps and
-eps +- h e_j) are thirteen FE_ONE_WAY points of one handle (stress only, homogenize.cpp:215-232), so they run
-as one batch and share the accepted history of the previous macro step.
+The FP64 solution comes from the library's FP64 load-path solver (micropp3_path_forward): FP64 Newton with
+the exact consistent tangent of the laws (forward-mode dual numbers), BiCGSTAB corrections to 1e-12 and the
+Newton residual to 1e-11 of its initial value, absolute stop off -- a solver that shares no code with the fast
+form's FP32 Jacobian, FP32 CG and implicit ctan beyond the FP64 residual and the laws.  The path takes the
+previous macro step (history strain) and accepts it, then the step to the strain checked.  Its ctan is exact
+in FP64 too: for L = sigma_k of the last step, the reverse-mode pass (micropp3_path_vjp) gives
+dL/d(strain of the last step) = row k of ctan, since that strain reaches sigma only through the last step's
+solve.  (A central difference of the stress is no good reference here: with a damage matrix, a step of
+h = 1e-7 in the strain moves some Gauss points across the loading/unloading switch or a kink of the softening
+curve, and on 60^3 RVEs that alone moved the difference by 1.2e-5 -- for every preconditioner alike.)
 
 Errors are relative to the largest entry of the FP64 tensor: max |a - b| / max |b|.
 """
 import numpy as np
 
-# Tolerances of the FP64 solution.
+# Tolerances of the FP64 solution (the path solver's BiCGSTAB stops at max(cg_rel_tol, 1e-14) of ||b||).
 TIGHT = dict(precision=0, ctan_mode=0, cg_rel_tol=1e-12, cg_abs_tol=1e-300, cg_max_its=20000, nr_rel_tol=1e-11,
              nr_max_tol=1e-30, nr_max_its=30, calc_ctan_lin=0, lin_stress=0)
-H = 1e-7
+H = 1e-7  # strain step of the central differences of the precision workload
 
 
 def rel_err(a, b):
@@ -24,36 +27,36 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b))) / s if s > 0 else float(np.max(np.abs(a)))
 
 
-def fp64_solution(n, mats, elem_type, history_strain, strain, h=H, **over):
-    """Stress and central-difference ctan at `strain` of an RVE whose history is that of `history_strain`,
-    accepted.  Returns (stress (6,), ctan (6, 6), statuses of the 13 solves, Newton iterations of the eps
-    solve)."""
+def fp64_solution(n, mats, elem_type, history_strain, strain, **over):
+    """FP64 stress and ctan at `strain` of an RVE whose previous step, to `history_strain`, was accepted (None:
+    no previous step), by the FP64 path solver and its reverse-mode pass.  Returns (stress (6,), ctan (6, 6),
+    status bits of the path's steps, Newton iterations of the last step)."""
     import micropp_gb300 as mg
     cfg = dict(TIGHT, **over)
-    r = mg.Micropp(mg.config(n, ngp=13, mats=mats, coupling=[mg.FE_ONE_WAY] * 13, elem_type=elem_type, **cfg))
+    strains = [strain] if history_strain is None else [history_strain, strain]
+    e = np.asarray(strains, dtype=np.float64).reshape(-1, 6)
+    ns = e.shape[0]
+    params = np.array([[m.E, m.nu, m.Xt, m.Sy, m.Ka] for m in mats])
+    r = mg.Micropp(mg.config(n, mats=mats, coupling=[mg.FE_FULL], elem_type=elem_type, **cfg))
     try:
-        if history_strain is not None:
-            for gp in range(13):
-                r.set_strain(gp, history_strain)
-            r.homogenize()
-            r.update_vars()
-        eps = np.asarray(strain, dtype=np.float64)
-        r.set_strain(0, eps)
-        for j in range(6):
-            d = np.zeros(6)
-            d[j] = h
-            r.set_strain(1 + 2 * j, eps + d)
-            r.set_strain(2 + 2 * j, eps - d)
-        r.homogenize()
-        stress = r.get_stress(0)
+        sig, rc = r.path_forward(e, params, checkpoint_every=ns)
+        if rc != 0:
+            raise RuntimeError(f"FP64 path solver returned {rc}")
+        newton = [r.path_newton(k) for k in range(ns)]
         ctan = np.zeros((6, 6))
-        for j in range(6):
-            ctan[:, j] = (r.get_stress(1 + 2 * j) - r.get_stress(2 + 2 * j)) / (2 * h)
-        status = [r.status(gp) for gp in range(13)]
-        newton = r.newton(0)
+        for k in range(6):
+            g = np.zeros((ns, 6))
+            g[-1, k] = 1.0
+            _, gs, rc = r.path_vjp(g)
+            if rc != 0:
+                raise RuntimeError(f"FP64 reverse pass returned {rc}")
+            ctan[k, :] = gs[-1]
     finally:
         r.close()
-    return stress, ctan, status, newton
+    # the path reports converged + 2 x (a linear solve stopped at its cap); as the library's status bits:
+    status = [(0 if nw[2] & 1 else mg.STATUS_NEWTON_MAX_ITS) | (mg.STATUS_CG_MAX_ITS if nw[2] & 2 else 0)
+              for nw in newton]
+    return sig[-1].copy(), ctan, status, newton[-1]
 
 
 def fast_solution(n, mats, elem_type, history_strains, strains, fast_cfg):
@@ -82,9 +85,10 @@ def compare(fast, fp64):
     per = []
     for (sf, cf, stf), (s64, c64, st64, nw) in zip(fast, fp64):
         per.append(dict(stress=rel_err(sf, s64), ctan=rel_err(cf, c64), fast_status=stf, fp64_status=max(st64),
-                        fp64_newton_its=nw[0]))
+                        fp64_newton_its=nw[0], fp64_rel_residual=nw[3]))
     return dict(stress=max(p["stress"] for p in per), ctan=max(p["ctan"] for p in per), rves=per,
-                reference=f"plain FP64 form, CG 1e-12, Newton 1e-11; ctan by central differences, h = {H:g}")
+                reference="FP64 path solver (exact tangent, BiCGSTAB 1e-12, Newton 1e-11); ctan by its reverse "
+                          "pass")
 
 
 def fast_vs_fp64(n, mats, elem_type, history_strains, strains, fast_cfg):

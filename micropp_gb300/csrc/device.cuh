@@ -69,7 +69,6 @@ struct Cg6State {
   double rz[6], pnorm0[6], pnorm[6], alpha[6], beta[6];
   double min_err, rel_err;
   int its, max_its, done[6], all_done, pad;
-  double ecorr[36];  // interior term of the energy form of ctan, sum over interior nodes of x_k . RF_i ([k * 6 + i])
 };
 
 // Small per-instance outputs read back by the host.

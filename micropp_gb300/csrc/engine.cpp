@@ -34,8 +34,8 @@ constexpr double kDepsCtanAve = 1.0e-8;        // params.hpp:32
 // until ||f_i - K x_i|| <= kTangentTol ||f_i|| for all six right-hand sides (at most kTangentSweeps sweeps).
 constexpr double kTangentSweepRel = 1.0e-5;
 constexpr double kTangentTol = 1.0e-9;
-// With a symmetric tangent (every phase elastic or damage) ctan takes the energy form, whose error is quadratic
-// in the solve's: the sweeps go to 2e-6 and the refinement stops at 3e-6 ||f_i||.
+// With a symmetric tangent (every phase elastic or damage) ctan takes the energy form from element energies,
+// whose error is quadratic in the solve's: the sweeps go to 2e-6 and the refinement stops at 3e-6 ||f_i||.
 constexpr double kTangentSweepRelEnergy = 2.0e-6;
 constexpr double kTangentTolEnergy = 3.0e-6;
 constexpr int kTangentSweeps = 4;
@@ -175,16 +175,6 @@ Engine::Engine(const micropp3_config &cfg) {
     d_dsh32_ = dalloc<float>(192, "dsh32");
     check(cudaMemcpy(d_dsh32_, dsh32, sizeof(dsh32), cudaMemcpyHostToDevice), "dsh32 upload");
   }
-  if (gather32_) {
-    std::vector<int> bn;
-    for (int n = 0; n < mesh_.nn; ++n) {
-      const int i = n % mesh_.nx, j = (n / mesh_.nx) % mesh_.ny, k = n / mesh_.nxny;
-      if (i == 0 || j == 0 || k == 0 || i == mesh_.nx - 1 || j == mesh_.ny - 1 || k == mesh_.nz - 1) bn.push_back(n);
-    }
-    nbnodes_ = (int)bn.size();
-    d_bnodes_ = dalloc<int>(bn.size(), "boundary nodes");
-    check(cudaMemcpy(d_bnodes_, bn.data(), bn.size() * sizeof(int), cudaMemcpyHostToDevice), "boundary nodes upload");
-  }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
   check(cudaMallocHost((void **)&h_chunks_, sizeof(unsigned int)), "pinned chunk count");
@@ -271,7 +261,6 @@ Engine::~Engine() {
   dfree(d_ke32_);
   dfree(d_k0g32_);
   dfree(d_dsh32_);
-  dfree(d_bnodes_);
   dfree(d_A0_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
@@ -1176,24 +1165,11 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
       }
     }
   }
-  if (energy) {
-    // The energy form's interior term needs the refinement residual of the final corrections: slots that left
-    // the loop at the sweep cap get theirs now (the others' is in R6 from their last check).
-    if (!live.empty()) {
-      upload_list(live);
-      launches_ += 1;
-      check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), 0, mg ? 1 : 0, stream_),
-                   "tangent residual");
-    }
-    upload_list(slots);
-    launches_ += 1;
-    check_launch(mgb_launch_t6_ecorr(&mesh_, d_insts_, d_list_, n, stream_), "ctan energy term");
-  }
   upload_list(slots);
   launches_ += 1;
   if (gather32_)
-    check_launch(mgb_launch_ctan_react(&mesh_, d_bnodes_, nbnodes_, d_insts_, d_list_, n, energy ? 1 : 0, stream_),
-                 "ctan reactions");
+    check_launch(mgb_launch_ctan_energy(&mesh_, &mats_, d_etype_, d_dsh32_, d_insts_, d_list_, n, stream_),
+                 "ctan (energy form)");
   else
     check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
   download_out();

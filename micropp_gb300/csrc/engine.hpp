@@ -249,8 +249,6 @@ class Engine {
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
   float *d_ke32_ = nullptr, *d_k0g32_ = nullptr, *d_dsh32_ = nullptr;
-  int *d_bnodes_ = nullptr;  // boundary nodes (gathered FP32 Jacobian: ctan from the boundary reactions)
-  int nbnodes_ = 0;
   std::vector<Slot> slots_;
   std::vector<Inst> h_insts_;
   Inst *d_insts_ = nullptr;

@@ -460,11 +460,11 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
 //   damage  (C_g = a_g C + c_g s_g s_g^T):  Ke_ab = sum_g a_g K0_g,ab + c_g wg (B_a,g^T s_g)(B_b,g^T s_g)^T
 //   elastic:                               Ke_ab = sum_g K0_g,ab
 // with K0_g = wg B_g^T C_phase B_g precomputed per phase and Gauss point, and (a_g, c_g, s_g) written by the
-// FP64 residual at the same displacement.  Each of the 8 warps of a block (one element position each, 32 node
-// rows) puts its 8 blocks per node into its own part of shared memory; after one barrier every entry of the 32
-// rows (27 slots x 9) is the sum of its element positions' blocks in the order ep = 0..7, written once,
-// coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their real rows.
+// FP64 residual at the same displacement.  The 8 warps of a block (one element position each) add their
+// blocks into the block's 32 node rows (27 slots x 9) in shared memory in a fixed order; the rows are then
+// written once, coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their real rows.
 constexpr int kAsmNodes = 32;
+constexpr int kAsmRow = kEllPerNode + 2;  // 245 floats: odd stride, conflict-free
 
 __host__ __device__ constexpr int corner_x(int b) { return ((b & 3) == 1 || (b & 3) == 2) ? 1 : 0; }
 __host__ __device__ constexpr int corner_y(int b) { return (b & 3) >= 2 ? 1 : 0; }
@@ -533,6 +533,17 @@ __device__ __forceinline__ void asm_ep(const MeshDev &m, const Mats &mats, const
   }
 }
 
+template <int EP>
+__device__ __forceinline__ void asm_store(const float (&acc)[8][9], float *row) {
+  constexpr int a = local_c(1 - (EP & 1), 1 - ((EP >> 1) & 1), 1 - (EP >> 2));
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const int sl = slot_of(corner_x(b) - corner_x(a), corner_y(b) - corner_y(a), corner_z(b) - corner_z(a));
+#pragma unroll
+    for (int q = 0; q < 9; ++q) row[sl * 9 + q] += acc[b][q];
+  }
+}
+
 #define MGB_EP_SWITCH(w, CALL) \
   switch (w) {                 \
     case 0: CALL(0); break;    \
@@ -545,17 +556,13 @@ __device__ __forceinline__ void asm_ep(const MeshDev &m, const Mats &mats, const
     default: CALL(7); break;   \
   }
 
-// Shared memory of k_asm_gather32: per warp (element position) 72 values (8 corner blocks x 9) of each of its
-// 32 nodes, lane-minor so that a warp's stores and the final pass' loads are conflict-free.
-constexpr size_t kAsmSmem = (size_t)8 * 72 * kAsmNodes * sizeof(float) + 8 * 24 * sizeof(float);
-
 __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_gather32(MeshDev m, Mats mats, const int8_t *etype,
                                                               const float *k0g, const float *kesum,
                                                               const float *dsh_g, const Inst *insts,
                                                               const int *list) {
-  extern __shared__ float asm_smem[];
-  float *part = asm_smem;                        // [ep][b * 9 + q][lane]
-  float *dsh = asm_smem + 8 * 72 * kAsmNodes;   // 8 x 24
+  __shared__ float rows[kAsmNodes * kAsmRow];
+  __shared__ float dsh[8 * 24];
+  for (int t = threadIdx.x; t < kAsmNodes * kAsmRow; t += blockDim.x) rows[t] = 0.f;
   for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
   __syncthreads();
   const Inst &I = insts[list[blockIdx.y]];
@@ -573,29 +580,19 @@ __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_gather32(MeshDev m, Mats 
     MGB_EP_SWITCH(w, MGB_ASM_CALL)
 #undef MGB_ASM_CALL
   }
-  float *mine = part + (size_t)w * 72 * kAsmNodes + lane;
-#pragma unroll
-  for (int b = 0; b < 8; ++b)
-#pragma unroll
-    for (int q = 0; q < 9; ++q) mine[(b * 9 + q) * kAsmNodes] = acc[b][q];
+  // element positions add into the node rows one after the other (fixed summation order)
+  for (int p = 0; p < 8; ++p) {
+    __syncthreads();
+    if (w == p && valid) {
+#define MGB_STORE_CALL(E) asm_store<E>(acc, &rows[lane * kAsmRow])
+      MGB_EP_SWITCH(w, MGB_STORE_CALL)
+#undef MGB_STORE_CALL
+    }
+  }
   __syncthreads();
-  // Entry E = slot * 9 + q of node lane: element position ep contributes its block toward corner b = a + d when
-  // the slot's offset d keeps a + d inside the element (a: the node's corner in that element).
   float *__restrict__ vals = I.vals32;
   const size_t np = m.np;
-  for (int E = w; E < kEllPerNode; E += 8) {
-    const int sl = E / 9, q = E % 9;
-    const int dx = sl % 3 - 1, dy = (sl / 3) % 3 - 1, dz = sl / 9 - 1;
-    float v = 0.f;
-#pragma unroll
-    for (int ep = 0; ep < 8; ++ep) {
-      const int ax = 1 - (ep & 1), ay = 1 - ((ep >> 1) & 1), az = 1 - (ep >> 2);
-      const int bx = ax + dx, by = ay + dy, bz = az + dz;
-      if (bx < 0 || bx > 1 || by < 0 || by > 1 || bz < 0 || bz > 1) continue;
-      v += part[((size_t)ep * 72 + local_c(bx, by, bz) * 9 + q) * kAsmNodes + lane];
-    }
-    vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = v;
-  }
+  for (int E = w; E < kEllPerNode; E += 8) vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = rows[lane * kAsmRow + E];
 }
 
 // Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
@@ -762,15 +759,8 @@ int mgb_launch_assembly_gather32(const MeshDev *m, const Mats *mats, const int8_
                               const float *kesum, const float *dsh32, const Inst *insts, const int *list, int nlist,
                               cudaStream_t s) {
   if (nlist <= 0) return 0;
-  static bool smem_set = false;  // the dynamic shared memory opt-in, once per process
-  if (!smem_set) {
-    const cudaError_t e = cudaFuncSetAttribute(k_asm_gather32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kAsmSmem);
-    if (e != cudaSuccess) return (int)e;
-    smem_set = true;
-  }
-  k_asm_gather32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, kAsmSmem, s>>>(*m, *mats, etype, k0g, kesum,
-                                                                                    dsh32, insts, list);
+  k_asm_gather32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, 0, s>>>(*m, *mats, etype, k0g, kesum, dsh32,
+                                                                             insts, list);
   return (int)cudaGetLastError();
 }
 

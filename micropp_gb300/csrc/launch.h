@@ -76,13 +76,10 @@ int mgb_launch_cg6_pupdate(const mgb::MeshDev *m, const mgb::Inst *insts, const 
                            unsigned int *active_count, cudaStream_t s);
 int mgb_launch_t6_accumulate(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist,
                              cudaStream_t s);
-// ctan from the boundary reactions of the tangent fields (gather-assembled FP32 Jacobian); bnodes lists the nbn
-// boundary nodes.
-// energy = 1: the energy form (symmetric tangents), with the interior term of mgb_launch_t6_ecorr.
-int mgb_launch_ctan_react(const mgb::MeshDev *m, const int *bnodes, int nbn, const mgb::Inst *insts, const int *list,
-                          int nlist, int energy, cudaStream_t s);
-// Interior term of the energy form of ctan from X6 and the last refinement residual in R6.
-int mgb_launch_t6_ecorr(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// ctan in the energy form from element energies (elastic and damage phases: a symmetric tangent).
+int mgb_launch_ctan_energy(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *dsh32,
+                           const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// ctan as the FP64 Gauss-point average of the tangent fields' stresses (a J2 phase: a non-symmetric tangent).
 int mgb_launch_ctan_avg(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 

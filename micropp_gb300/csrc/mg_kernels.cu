@@ -566,9 +566,10 @@ __global__ void __launch_bounds__(B, 512 / B) k_mg_resid6(MeshDev m, const Inst 
 
 // Level-0 post-smoother of the 6-RHS V-cycle with the pair structure of k_mg_resid6: z = t0 + w D^-1 (r - A t0)
 // and rz_i = sum r.z for two consecutive nodes per thread; setup: p = z.  The CG scalars as in k_mg_post0.
-// Bounded to 384 threads per SM (about 168 registers): at 128 registers it spills.
+// Bounded to 512 threads per SM like k_mg_resid6 (128 registers; a few words spill to L1): at one 256-thread
+// block per SM its loads had too little parallelism.
 template <int B, bool HALF>
-__global__ void __launch_bounds__(B, 384 / B) k_mg_post06(MeshDev m, const Inst *insts, const int *list,
+__global__ void __launch_bounds__(B, 512 / B) k_mg_post06(MeshDev m, const Inst *insts, const int *list,
                                                           float omega, int setup) {
   const Inst &I = insts[list[blockIdx.y]];
   if (I.cg6->all_done) return;

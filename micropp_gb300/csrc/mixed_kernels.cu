@@ -645,111 +645,131 @@ __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
     for (int c = 0; c < 18; ++c) X6[(size_t)c * np + n] += (double)D6[(size_t)c * np + n];
 }
 
-// ctan by boundary reactions (FP32 Jacobian assembled by node gather, which stores the boundary rows).  Column i of ctan
-// is the volume-average stress of the tangent field u_i = w_i + x_i, and for any displacement field
-//   integral of sigma = sum over all nodes n of f_n (x) X_n,   f_n = (K u)_n,
-// because the nodal gradients of the shape functions weighted by the nodal coordinates sum to the identity.
-// On interior rows f_n = -RF_n, the final refinement residual (below the tangent tolerance), so the sum runs
-// over the boundary nodes; the shear entries take the symmetric part.  One thread per boundary node, FP64
-// accumulation of the FP32 matrix values.
-//
-// energy = 1 (symmetric tangent): ctan[k][i] = (1/V) v_k^T K v_i with v = w + x, the energy form, whose error is
-// quadratic in the error of x where the boundary sum's is linear.  With (K v_i) = -RF_i on interior rows it is
-// the boundary sum minus (1/V) sum over interior nodes of x_k . RF_i (Cg6State::ecorr, k_t6_ecorr).
-__global__ void __launch_bounds__(kNodeBlock) k_ctan_react(MeshDev m, const int *bnodes, int nbn, const Inst *insts,
-                                                           const int *list, int energy) {
-  const Inst &I = insts[list[blockIdx.y]];
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[36];
-#pragma unroll
-  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
-  if (t < nbn) {
-    const int n = bnodes[t];
-    int i, j, k;
-    bnd(m, n, i, j, k);
-    double X[3];
-    bc_coords(m, i, j, k, X);
-    const size_t np = m.np;
-    double f[6][3];
-#pragma unroll
-    for (int r = 0; r < 6; ++r) f[r][0] = f[r][1] = f[r][2] = 0.0;
-#pragma unroll 1
-    for (int s = 0; s < 27; ++s) {
-      const int di = s % 3 - 1, dj = (s / 3) % 3 - 1, dk = s / 9 - 1;
-      const int ii = i + di, jj = j + dj, kk = k + dk;
-      if (ii < 0 || jj < 0 || kk < 0 || ii >= m.nx || jj >= m.ny || kk >= m.nz) continue;
-      const int nb = n + dk * m.nxny + dj * m.nx + di;
-      double Kb[9];
-      ell32_block(m, I.vals32, n, s, Kb);
-      int bi, bj, bk;
-      const bool nbb = bnd(m, nb, bi, bj, bk);
-      double c[3];
-      if (nbb) bc_coords(m, bi, bj, bk, c);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        double u[3];
-        if (nbb) {
-          lift(c, r, u);
-        } else {
-#pragma unroll
-          for (int d = 0; d < 3; ++d) u[d] = I.X6[c6(r, d, np) + nb];
-        }
-#pragma unroll
-        for (int fi = 0; fi < 3; ++fi) f[r][fi] += Kb[fi * 3] * u[0] + Kb[fi * 3 + 1] * u[1] + Kb[fi * 3 + 2] * u[2];
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      acc[0 * 6 + r] = f[r][0] * X[0];
-      acc[1 * 6 + r] = f[r][1] * X[1];
-      acc[2 * 6 + r] = f[r][2] * X[2];
-      acc[3 * 6 + r] = 0.5 * (f[r][0] * X[1] + f[r][1] * X[0]);
-      acc[4 * 6 + r] = 0.5 * (f[r][0] * X[2] + f[r][2] * X[0]);
-      acc[5 * 6 + r] = 0.5 * (f[r][1] * X[2] + f[r][2] * X[1]);
-    }
-  }
-  double tot[36];
-  if (grid_sum<36>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
-    bool bad = false;
-    for (int q = 0; q < 36; ++q) {
-      const double t = energy ? tot[q] - I.cg6->ecorr[q] : tot[q];
-      I.out->ctan[q] = t / m.vol_tot;
-      bad |= !isfinite(t);
-    }
-    if (bad) I.out->nonfinite = 1;
-  }
-}
+// ctan in the energy form, element by element (FP32 Jacobian assembled by node gather: elastic and damage
+// phases, a symmetric tangent).  With v_i = w_i + x_i the tangent field of unit strain i (w_i the boundary lift,
+// x_i the interior solution X6),
+//   ctan[k][i] = (1/V) sum_e sum_g wg eps(v_k)^T C_g eps(v_i),
+// C_g the Gauss-point tangent: the phase's elastic C, or for damage a C + c s s^T from the tangent terms the FP64
+// residual wrote.  The form is stationary at the exact x, so its error is quadratic in the error of x (the FP32
+// solves and the FP32 rounding of the assembled tangent they used).  Summing element energies also avoids the
+// cancellation of v^T (K v) over assembled rows -- K v nearly vanishes on interior rows -- whose first-order
+// rounding with FP32 rows reached 1e-5 on 60^3 RVEs.  Block: kEnElems elements x 8 threads.  Thread a of an
+// element loads node a's six fields in FP64 and keeps their differences from node 0 in FP32 (the strains
+// need only differences: sum_a dN_a = 0); then, as Gauss point g, it forms the six strains, the tangent
+// products and the 21 energies.  FP32 per element, FP64 across elements.
+constexpr int kEnElems = 32;
+constexpr int kEnStride = 7 * 18 + 1;  // differences of nodes 1..7, 6 fields x 3; odd stride
 
-// Interior term of the energy form of ctan: ecorr[k * 6 + i] = sum over interior nodes of x_k . RF_i, with x the
-// tangent corrections (X6) and RF_i the refinement residual of the final X6 as k_t6_residual left it in R6 (its
-// FP32 rounding only moves this correction term by ~1e-7 of itself).  One thread per node, FP64 sums.
-__global__ void __launch_bounds__(kNodeBlock) k_t6_ecorr(MeshDev m, const Inst *insts, const int *list) {
+__global__ void __launch_bounds__(kEnElems * 8) k_ctan_energy(MeshDev m, Mats mats, const int8_t *etype,
+                                                             const float *dsh_g, const Inst *insts, const int *list) {
+  __shared__ float dv[kEnElems * kEnStride];
+  __shared__ float dsh[8 * 24];
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) dsh[t] = dsh_g[t];
   const Inst &I = insts[list[blockIdx.y]];
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[36];
+  const int el = threadIdx.x >> 3, sub = threadIdx.x & 7;  // sub: the node (loads), then the Gauss point
+  const int e = blockIdx.x * kEnElems + el;
+  const bool valid = e < m.nelem;
+  const size_t np = m.np;
+  double v[18];
 #pragma unroll
-  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
-  if (n < m.nn) {
-    int i, j, k;
-    if (!bnd(m, n, i, j, k)) {
-      const size_t np = m.np;
-      double x[6][3], rf[6][3];
+  for (int q = 0; q < 18; ++q) v[q] = 0.0;
+  if (valid) {
+    const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
+    const int n = (ez + c_corner6[sub][2]) * m.nxny + (ey + c_corner6[sub][1]) * m.nx + ex + c_corner6[sub][0];
+    int bi, bj, bk;
+    if (bnd(m, n, bi, bj, bk)) {
+      double X[3];
+      bc_coords(m, bi, bj, bk, X);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) lift(X, r, &v[r * 3]);
+    } else {
 #pragma unroll
       for (int r = 0; r < 6; ++r)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          x[r][d] = I.X6[c6(r, d, np) + n];
-          rf[r][d] = (double)I.R6[c6(r, d, np) + n];
-        }
-#pragma unroll
-      for (int a = 0; a < 6; ++a)
-#pragma unroll
-        for (int b = 0; b < 6; ++b) acc[a * 6 + b] = x[a][0] * rf[b][0] + x[a][1] * rf[b][1] + x[a][2] * rf[b][2];
+        for (int d = 0; d < 3; ++d) v[r * 3 + d] = I.X6[c6(r, d, np) + n];
     }
   }
-  double tot[36];
-  if (grid_sum<36>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
-    for (int q = 0; q < 36; ++q) I.cg6->ecorr[q] = tot[q];
+  const int lane0 = (threadIdx.x & 31) & ~7;  // node 0 of this element, in the same warp
+#pragma unroll
+  for (int q = 0; q < 18; ++q) {
+    const double v0 = __shfl_sync(0xffffffffu, v[q], lane0);
+    if (sub > 0) dv[el * kEnStride + (sub - 1) * 18 + q] = (float)(v[q] - v0);
+  }
+  __syncthreads();
+  float acc[21];
+#pragma unroll
+  for (int q = 0; q < 21; ++q) acc[q] = 0.f;
+  if (valid) {
+    const float *dg = dsh + sub * 24;
+    const float *dve = dv + el * kEnStride;
+    float eps[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) eps[r][c] = 0.f;
+#pragma unroll
+    for (int a = 1; a < 8; ++a) {
+      const float gx = dg[a * 3], gy = dg[a * 3 + 1], gz = dg[a * 3 + 2];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const float ux = dve[(a - 1) * 18 + r * 3], uy = dve[(a - 1) * 18 + r * 3 + 1],
+                    uz = dve[(a - 1) * 18 + r * 3 + 2];
+        eps[r][0] = fmaf(gx, ux, eps[r][0]);
+        eps[r][1] = fmaf(gy, uy, eps[r][1]);
+        eps[r][2] = fmaf(gz, uz, eps[r][2]);
+        eps[r][3] = fmaf(gy, ux, fmaf(gx, uy, eps[r][3]));
+        eps[r][4] = fmaf(gz, ux, fmaf(gx, uz, eps[r][4]));
+        eps[r][5] = fmaf(gz, uy, fmaf(gy, uz, eps[r][5]));
+      }
+    }
+    const MatDev &md = mats.m[etype[e]];
+    float ta = 1.f, tc = 0.f, s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (md.type == 2) {
+      const size_t st = (size_t)8 * m.nelem, o = (size_t)sub * m.nelem + e;
+      ta = I.gpd[o];
+      tc = I.gpd[st + o];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) s[q] = I.gpd[(2 + q) * st + o];
+    }
+    const float lam = (float)md.lambda, mu = (float)md.mu, w = (float)m.wg;
+    float sig[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const float tr = eps[r][0] + eps[r][1] + eps[r][2];
+      float se = 0.f;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) se = fmaf(s[q], eps[r][q], se);
+      se *= tc;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const float el_q = (q < 3) ? lam * tr + 2.f * mu * eps[r][q] : mu * eps[r][q];
+        sig[r][q] = fmaf(ta, el_q, se * s[q]);
+      }
+    }
+    int q = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int i = k; i < 6; ++i) {
+        float en = 0.f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) en = fmaf(eps[i][c], sig[k][c], en);
+        acc[q++] = w * en;
+      }
+  }
+  double tot[21];
+  if (grid_sum_f<21>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+    bool bad = false;
+    int q = 0;
+    for (int k = 0; k < 6; ++k)
+      for (int i = k; i < 6; ++i) {
+        const double c = tot[q++] / m.vol_tot;
+        I.out->ctan[k * 6 + i] = c;
+        I.out->ctan[i * 6 + k] = c;
+        bad |= !isfinite(c);
+      }
+    if (bad) I.out->nonfinite = 1;
+  }
 }
 
 // ctan[v][i] = (1/V) sum over Gauss points of wg (C_gp B (w_i + x_i))_v, one thread per Gauss point, FP64.
@@ -982,16 +1002,10 @@ int mgb_launch_t6_accumulate(const MeshDev *m, const Inst *insts, const int *lis
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_ctan_react(const MeshDev *m, const int *bnodes, int nbn, const Inst *insts, const int *list, int nlist,
-                          int energy, cudaStream_t s) {
-  if (nlist <= 0 || nbn <= 0) return 0;
-  k_ctan_react<<<dim3(cdiv(nbn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, bnodes, nbn, insts, list, energy);
-  return (int)cudaGetLastError();
-}
-
-int mgb_launch_t6_ecorr(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_ctan_energy(const MeshDev *m, const Mats *mats, const int8_t *etype, const float *dsh32,
+                           const Inst *insts, const int *list, int nlist, cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_ecorr<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_ctan_energy<<<dim3(cdiv(m->nelem, kEnElems), nlist), kEnElems * 8, 0, s>>>(*m, *mats, etype, dsh32, insts, list);
   return (int)cudaGetLastError();
 }
 

@@ -526,7 +526,7 @@ static void ell_mvp(const orc_ell *m, const double *x, double *y) {
 /* get_dot (ell.cpp:53-57).  With -DORC_BLOCKED_DOTS the sum is taken in blocks of 768 terms whose partial
  * sums are added last, the association of a GPU grid reduction; that build only serves to measure how much
  * a different summation order moves the results (tests/test_rounding_floor.py). */
-static double get_dot(const double *a, const double *b, int n) {
+__attribute__((unused)) static double get_dot(const double *a, const double *b, int n) {
 #ifdef ORC_BLOCKED_DOTS
   double total = 0.0;
   for (int i0 = 0; i0 < n; i0 += 768) {

@@ -3,9 +3,10 @@
 Three RVEs of the headline workload (4 stiff layers normal to z in a damage matrix, the bench's seeded
 strain targets): the previous step at half the target accepted, then stress + ctan at the target.  The fast
 form (FP32 Jacobian and CG in FP64 refinement, implicit ctan), with the multigrid (FP32 or FP16 smoothing
-operator) and with the Jacobi preconditioner, is held to the bars the fast form states: average stress within 1e-7 and ctan within 1e-5
-(relative to the largest entry) of the plain FP64 form converged to CG 1e-12 / Newton 1e-11, whose ctan is a
-central difference with h = 1e-7 (micropp_gb300.accuracy).
+operator) and with the Jacobi preconditioner, is held to the bars the fast form states: average stress
+within 1e-7 and ctan within 1e-5 (relative to the largest entry) of the FP64 solution: the library's FP64
+path solver (exact tangent, BiCGSTAB, Newton to 1e-11) and the exact FP64 ctan of its reverse-mode pass
+(micropp_gb300.accuracy).
 """
 import pytest
 

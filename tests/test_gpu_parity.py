@@ -88,10 +88,12 @@ def test_fe_linear_next_to_fe_full_and_homogenize_linear(gpu_lib):
     g.homogenize_linear()
     o.homogenize_linear()
     for gp in range(3):
-        assert rel_err(g.get_stress(gp), o.get_stress(gp)) < TOL_STRESS
-        assert rel_err(g.get_stress(gp), ref["stress_linear"][gp]) < TOL_STRESS
-        # the linear pass leaves ctan as it was
-        assert rel_err(g.get_ctan(gp), o.get_ctan(gp)) < (TOL_CTAN if o.is_non_linear(gp) else TOL_CTAN_LIN)
+        # stress = ctan strain: held to the tolerance of the point's ctan (a nonlinear point's is a forward
+        # difference, see the module docstring); the linear pass leaves ctan as it was
+        tol = TOL_CTAN if o.is_non_linear(gp) else TOL_CTAN_LIN
+        assert rel_err(g.get_stress(gp), o.get_stress(gp)) < tol
+        assert rel_err(g.get_stress(gp), ref["stress_linear"][gp]) < tol
+        assert rel_err(g.get_ctan(gp), o.get_ctan(gp)) < tol
 
 
 def test_damage_layers_two_points(gpu_lib):

@@ -92,3 +92,18 @@ def test_floor_j2_ctan_above_1e8(fma_oracle):
     w = spread(fma_oracle, "plastic_sphere")
     assert w["stress"] < 1e-12
     assert 1e-9 < w["ctan"] < 1e-7, w
+
+
+@pytest.fixture(scope="module")
+def gpuorder_oracle(tmp_path_factory):
+    return _variant(tmp_path_factory, "gpuorder", ["-ffp-contract=off", "-DORC_GPU_ORDER"])
+
+
+@pytest.mark.parametrize("name", ["damage_layers", "plastic_sphere"])
+def test_floor_gpu_reduction_order(gpuorder_oracle, name):
+    """The reference algorithm with the GPU library's CG reduction tree and colour-ordered assembly: the same
+    costs, stress to ~1e-13, and the forward-difference ctan moved by up to ~1e-7 -- the floor against which
+    the GPU's nonlinear ctan is held (tests/test_gpu_rounding_floor.py)."""
+    w = spread(gpuorder_oracle, name)
+    assert w["stress"] < 1e-12, w
+    assert w["ctan"] < 1e-6, w
