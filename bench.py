@@ -459,7 +459,8 @@ def measure_form(args, form, et, xts, targets, L, pg, world, local):
     launches = sum(h.kernel_launches() for h in handles) - l0
     last_s, last_c = out_s.copy(), out_c.copy()  # results of the last timed step
     stats = {}
-    for fam in ("spmv", "spmv6", "cg_update", "cg6_update", "mg", "mg6", "mg_coarse", "assembly", "residual"):
+    for fam in ("spmv", "spmv6", "cg_update", "cg6_update", "mg", "mg6", "mg_coarse", "assembly", "mg_rap", "residual",
+                "tangent"):
         tot = [h.kernel_stats(fam) for h in handles]
         stats[fam] = (sum(t[0] for t in tot), sum(t[1] for t in tot), sum(t[2] for t in tot))
     status = [h.status(gp) for h, gp in points]

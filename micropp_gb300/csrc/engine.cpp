@@ -250,7 +250,8 @@ Engine::~Engine() {
   clear_graphs();
   path_free();
   free_slots();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_})
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_, &t_rap_,
+                          &t_tan_})
     for (auto &e : t->pool) {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
@@ -783,7 +784,8 @@ void Engine::timer_end(KernelTimer &t) {
 
 void Engine::set_kernel_timing(bool on) {
   sync();
-  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_}) {
+  for (KernelTimer *t : {&t_spmv_, &t_update_, &t_asm_, &t_res_, &t_spmv6_, &t_upd6_, &t_mg1_, &t_mg6_, &t_mgc_, &t_rap_,
+                          &t_tan_}) {
     t->enabled = on;
     t->used = 0;
     t->launches = 0;
@@ -796,6 +798,8 @@ bool Engine::kernel_stats(const std::string &family, long *launches, double *ms,
   if (family == "spmv") t = &t_spmv_;
   else if (family == "cg_update") t = &t_update_;
   else if (family == "assembly") t = &t_asm_;
+  else if (family == "mg_rap") t = &t_rap_;
+  else if (family == "tangent") t = &t_tan_;
   else if (family == "residual") t = &t_res_;
   else if (family == "spmv6") t = &t_spmv6_;
   else if (family == "cg6_update") t = &t_upd6_;
@@ -969,7 +973,7 @@ void Engine::mg_rap(int nlist) {
       bytes += 4.0 * kEllPerNode * ((double)f.np + 2.0 * n1 + 2.0 * n2 + (double)c.np);
     }
   }
-  timer_begin(t_asm_, nlist * bytes);
+  timer_begin(t_rap_, nlist * bytes);
   launches_ += 1;
   check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
                "multigrid smoother diagonal");
@@ -988,7 +992,7 @@ void Engine::mg_rap(int nlist) {
     check_launch(mgb_launch_mg_sdiag(&c, d_insts_, d_list_, nlist, lf + 1, kMgOmega, kMgSafe, stream_),
                  "multigrid smoother diagonal");
   }
-  timer_end(t_asm_);
+  timer_end(t_rap_);
 }
 
 // Algorithmic bytes of one V-cycle per instance.  Level 0: the residual and the post-smoother, each 81 values
@@ -1072,7 +1076,9 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
   upload_list(slots);
   assemble32(n);
   launches_ += 1;
+  timer_begin(t_tan_, 0.0);
   check_launch(mgb_launch_t6_rhs(&mesh_, d_insts_, d_list_, n, stream_), "tangent rhs");
+  timer_end(t_tan_);
   const double nrow = (double)nndim();
   // Per iteration and instance: SpMV 81 values per row, 6 x read and 6 y written; update: read P, AP, R, D,
   // write D, R, Z; p-update: read Z, P, write P (per right-hand side).  Credited per instance iteration.
@@ -1092,9 +1098,11 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
     }
     if (sweep > 0) upload_list(live);
     launches_ += 1;
+    timer_begin(t_tan_, 0.0);
     check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
                                         mg ? 1 : 0, stream_),
                  "tangent residual");
+    timer_end(t_tan_);
     download_out();
     std::vector<int> next, next_idx;
     for (size_t a = 0; a < live.size(); ++a) {
@@ -1120,9 +1128,11 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
         check(cudaMemcpyAsync(slots_[s].cg6, &c, sizeof(Cg6State), cudaMemcpyHostToDevice, stream_), "cg6 init");
       }
       launches_ += 1;
+      timer_begin(t_tan_, 0.0);
       check_launch(mgb_launch_t6_residual(&mesh_, d_insts_, d_list_, (int)live.size(), sweep == 0 ? 1 : 0,
                                           mg ? 1 : 0, stream_),
                    "tangent residual");
+      timer_end(t_tan_);
     }
     const int nl = (int)live.size();
     const int block = tuned_block(1, nl);
@@ -1151,7 +1161,9 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
       if (*h_count_ == 0) break;
     }
     launches_ += 1;
+    timer_begin(t_tan_, 0.0);
     check_launch(mgb_launch_t6_accumulate(&mesh_, d_insts_, d_list_, nl, stream_), "tangent accumulate");
+    timer_end(t_tan_);
     download_out();
     for (size_t a = 0; a < live.size(); ++a) {
       its[live_idx[a]] += h_out_[live[a]].cg6_its;
@@ -1167,11 +1179,16 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
   }
   upload_list(slots);
   launches_ += 1;
-  if (gather32_)
+  if (gather32_) {
+    timer_begin(t_tan_, 0.0);
     check_launch(mgb_launch_ctan_energy(&mesh_, &mats_, d_etype_, d_dsh32_, d_insts_, d_list_, n, stream_),
                  "ctan (energy form)");
-  else
+    timer_end(t_tan_);
+  } else {
+    timer_begin(t_tan_, 0.0);
     check_launch(mgb_launch_ctan_avg(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, n, stream_), "ctan average");
+    timer_end(t_tan_);
+  }
   download_out();
   if (mg) {
     // Slots whose multigrid sweeps reached the iteration cap are solved again with Jacobi, from the start.

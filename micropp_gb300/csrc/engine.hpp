@@ -260,6 +260,8 @@ class Engine {
   long total_cg_its_ = 0;
   long launches_ = 0;  // kernels of this library launched by the handle
   KernelTimer t_spmv_, t_update_, t_asm_, t_res_, t_spmv6_, t_upd6_;
+  KernelTimer t_rap_;  // multigrid operators after an assembly: smoother diagonals and Galerkin products
+  KernelTimer t_tan_;  // FP64 kernels of the implicit ctan: right-hand sides, refinement residuals, ctan sums
   KernelTimer t_mg1_, t_mg6_, t_mgc_;  // V-cycles: level-0 passes (1 and 6 RHS), coarse levels and transfers
   PathState path_;
   bool graphs_ = true;                         // CG chunks replayed from captured CUDA graphs
