@@ -119,8 +119,8 @@ struct Inst {
   // Gauss-point tangent descriptors of the damage law for the symmetric FP32 Jacobian, written by the FP64
   // residual: [(q * 8 + g) * nelem + e], q = 0: a, 1: c, 2..7: s  (C_gp = a C_el + c s s^T)
   float *gpd;
-  // implicit ctan: 6 right-hand sides
-  double *X6, *F6;
+  // implicit ctan: 6 right-hand sides; X6 (solutions) and F6 (right-hand sides) as double-float pairs hi + lo
+  float *X6h, *X6l, *F6h, *F6l;
   float *R6, *Z6, *P6, *AP6, *D6;
   Cg6State *cg6;
   MgInst *mg;              // multigrid hierarchy (NULL: Jacobi-preconditioned CG)

@@ -175,6 +175,20 @@ Engine::Engine(const micropp3_config &cfg) {
     d_dsh32_ = dalloc<float>(192, "dsh32");
     check(cudaMemcpy(d_dsh32_, dsh32, sizeof(dsh32), cudaMemcpyHostToDevice), "dsh32 upload");
   }
+  {
+    // interior nodes with a boundary neighbour: the rows of the tangent right-hand sides f_i = -K_IB w_i
+    std::vector<int> near;
+    for (int k = 1; k < mesh_.nz - 1; ++k)
+      for (int j = 1; j < mesh_.ny - 1; ++j)
+        for (int i = 1; i < mesh_.nx - 1; ++i)
+          if (i == 1 || j == 1 || k == 1 || i == mesh_.nx - 2 || j == mesh_.ny - 2 || k == mesh_.nz - 2)
+            near.push_back((k * mesh_.ny + j) * mesh_.nx + i);
+    nnear_ = (int)near.size();
+    if (nnear_ > 0) {
+      d_near_ = dalloc<int>(near.size(), "near-boundary nodes");
+      check(cudaMemcpy(d_near_, near.data(), near.size() * sizeof(int), cudaMemcpyHostToDevice), "near upload");
+    }
+  }
   check(cudaMallocHost((void **)&h_count_, sizeof(unsigned int)), "pinned count");
   d_count_ = dalloc<unsigned int>(1, "count");
   check(cudaMallocHost((void **)&h_chunks_, sizeof(unsigned int)), "pinned chunk count");
@@ -262,6 +276,7 @@ Engine::~Engine() {
   dfree(d_ke32_);
   dfree(d_k0g32_);
   dfree(d_dsh32_);
+  dfree(d_near_);
   dfree(d_A0_);
   dfree(d_count_);
   if (h_count_) cudaFreeHost(h_count_);
@@ -517,8 +532,10 @@ void Engine::ensure_slots(int n) {
     }
     if (implicit) {
       const size_t n6 = (size_t)18 * mesh_.np;  // six right-hand sides, component-major
-      w.X6 = dalloc<double>(n6, "X6");
-      w.F6 = dalloc<double>(n6, "F6");
+      w.X6h = dalloc<float>(n6, "X6 (hi)");
+      w.X6l = dalloc<float>(n6, "X6 (lo)");
+      w.F6h = dalloc<float>(n6, "F6 (hi)");
+      w.F6l = dalloc<float>(n6, "F6 (lo)");
       w.R6 = dalloc<float>(n6, "R6");
       w.Z6 = dalloc<float>(n6, "Z6");
       w.P6 = dalloc<float>(n6, "P6");
@@ -584,7 +601,7 @@ void Engine::ensure_slots(int n) {
     I.vals = w.vals; I.be = w.be; I.red = w.red; I.ticket = w.ticket; I.cg = w.cg; I.out = w.out;
     I.vals32 = w.vals32; I.kinv32 = w.kinv32; I.r32 = w.r32; I.z32 = w.z32; I.p32 = w.p32; I.Ap32 = w.Ap32;
     I.du32 = w.du32;
-    I.X6 = w.X6; I.F6 = w.F6; I.R6 = w.R6; I.Z6 = w.Z6; I.P6 = w.P6; I.AP6 = w.AP6; I.D6 = w.D6; I.cg6 = w.cg6;
+    I.X6h = w.X6h; I.X6l = w.X6l; I.F6h = w.F6h; I.F6l = w.F6l; I.R6 = w.R6; I.Z6 = w.Z6; I.P6 = w.P6; I.AP6 = w.AP6; I.D6 = w.D6; I.cg6 = w.cg6;
     I.gpd = w.gpd;
     I.mg = w.mg;
     I.vars_old = nullptr;
@@ -599,9 +616,9 @@ void Engine::ensure_slots(int n) {
 
 void Engine::free_slots() {
   for (auto &w : slots_) {
-    for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red, w.X6, w.F6})
-      dfree(p);
-    for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6, w.gpd})
+    for (double *p : {w.u, w.du, w.b, w.r, w.z, w.p, w.Ap, w.kinv, w.vals, w.be, w.vars_aux, w.red}) dfree(p);
+    for (float *p : {w.vals32, w.kinv32, w.r32, w.z32, w.p32, w.Ap32, w.du32, w.R6, w.Z6, w.P6, w.AP6, w.D6, w.gpd,
+                     w.X6h, w.X6l, w.F6h, w.F6l})
       dfree(p);
     for (float *p : w.mg_bufs) dfree(p);
     w.mg_bufs.clear();
@@ -833,7 +850,7 @@ void Engine::residual(const std::vector<int> &slots) {
   timer_begin(t_res_, bytes);
   launches_ += 2;
   check_launch(mgb_launch_residual(&mesh_, &mats_, d_etype_, d_dsh_, d_insts_, d_list_, (int)slots.size(),
-                                   precision_ == MICROPP3_FP64 ? 1 : 0, stream_),
+                                   precision_ == MICROPP3_FP64 ? 1 : (gather32_ ? 2 : 0), stream_),
                "residual");
   timer_end(t_res_);
 }
@@ -1075,9 +1092,9 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
   upload_insts();
   upload_list(slots);
   assemble32(n);
-  launches_ += 1;
+  launches_ += 2;
   timer_begin(t_tan_, 0.0);
-  check_launch(mgb_launch_t6_rhs(&mesh_, d_insts_, d_list_, n, stream_), "tangent rhs");
+  check_launch(mgb_launch_t6_rhs(&mesh_, d_near_, nnear_, d_insts_, d_list_, n, stream_), "tangent rhs");
   timer_end(t_tan_);
   const double nrow = (double)nndim();
   // Per iteration and instance: SpMV 81 values per row, 6 x read and 6 y written; update: read P, AP, R, D,

@@ -43,7 +43,7 @@ struct Slot {
   double *kinv = nullptr, *vals = nullptr, *be = nullptr, *vars_aux = nullptr, *red = nullptr;
   float *vals32 = nullptr, *kinv32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr,
         *du32 = nullptr;
-  double *X6 = nullptr, *F6 = nullptr;
+  float *X6h = nullptr, *X6l = nullptr, *F6h = nullptr, *F6l = nullptr;  // double-float pairs
   float *R6 = nullptr, *Z6 = nullptr, *P6 = nullptr, *AP6 = nullptr, *D6 = nullptr;
   float *gpd = nullptr;
   MgInst *mg = nullptr;          // device copy of the multigrid hierarchy's pointers
@@ -249,6 +249,8 @@ class Engine {
   int8_t *d_etype_ = nullptr;
   double *d_dsh_ = nullptr, *d_ke_ = nullptr;
   float *d_ke32_ = nullptr, *d_k0g32_ = nullptr, *d_dsh32_ = nullptr;
+  int *d_near_ = nullptr;  // interior nodes with a boundary neighbour, ascending
+  int nnear_ = 0;
   std::vector<Slot> slots_;
   std::vector<Inst> h_insts_;
   Inst *d_insts_ = nullptr;

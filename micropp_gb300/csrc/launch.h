@@ -18,10 +18,11 @@ extern "C" {
 int mgb_launch_set_bc(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_add_du(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 int mgb_launch_copy(int n, const double *const *src, double *const *dst, const int *list, int nlist, cudaStream_t s);
-// ref_order: the element residual by B-matrix products in the reference's order (the FP64 form); otherwise by
-// sum factorisation (the mixed form).
+// form: 1 = the element residual by B-matrix products in the reference's order (the FP64 form); 0 = by sum
+// factorisation in FP64 (the mixed form with a J2 phase); 2 = by sum factorisation in double-float arithmetic
+// (the mixed form with elastic and damage phases only).
 int mgb_launch_residual(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
-                        const mgb::Inst *insts, const int *list, int nlist, int ref_order, cudaStream_t s);
+                        const mgb::Inst *insts, const int *list, int nlist, int form, cudaStream_t s);
 int mgb_launch_assembly(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const double *dsh,
                         const double *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 // FP64 Jacobian with the exact Gauss-point tangents (forward-mode dual numbers), for the adjoint.
@@ -65,7 +66,9 @@ int mgb_launch_zero_u32(unsigned int *p, cudaStream_t s);
 int mgb_launch_cg_continue(cudaGraphConditionalHandle h, const unsigned int *count, unsigned int *chunks,
                            unsigned int cap, cudaStream_t s);
 int mgb_launch_axpy_du32(const mgb::MeshDev *m, double *u, const float *du, double a, cudaStream_t s);
-int mgb_launch_t6_rhs(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
+// near: the interior nodes with a boundary neighbour (the only nonzero rows of f_i = -K_IB w_i), nnear of them.
+int mgb_launch_t6_rhs(const mgb::MeshDev *m, const int *near, int nnear, const mgb::Inst *insts, const int *list,
+                      int nlist, cudaStream_t s);
 int mgb_launch_t6_residual(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int x_zero,
                            int mg, cudaStream_t s);
 int mgb_launch_cg6_spmv(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int block,

@@ -10,13 +10,15 @@
 //   du/deps_i = w_i + x_i,   K_II x_i = f_i = -K_IB w_i,
 // where w_i is the affine boundary field of the unit strain e_i (micro3D.cpp:26-78 with eps = e_i) and x_i
 // vanishes on the boundary.  The six systems are solved together (one pass over K per iteration serves all
-// six) by FP32 CG, refined with FP64 residuals f_i - K x_i, and
-//   ctan[v][i] = (1/V) sum_e sum_gp wg (C_gp B (w_i + x_i)_e)_v
-// is accumulated in FP64.  This replaces the six perturbed Newton solves of homogenize.cpp:256-275.
+// six) by FP32 CG, refined with residuals f_i - K x_i in double-float arithmetic (x_i and f_i are held as pairs
+// of floats, hi + lo), and ctan follows from the tangent fields w_i + x_i: as the element-energy sum (elastic and
+// damage phases) or the FP64 Gauss-point average of C_gp B (w_i + x_i) (a J2 phase).  This replaces the six
+// perturbed Newton solves of homogenize.cpp:256-275.
 #include <cuda_runtime.h>
 
 #include "bc.cuh"
 #include "device.cuh"
+#include "df.cuh"
 #include "launch.h"
 #include "laws.cuh"
 #include "reduce.cuh"
@@ -42,6 +44,24 @@ __device__ __forceinline__ void ell32_block(const MeshDev &m, const float *__res
 // Entry index of diagonal entry (d, d) of row n's own block in the FP32 ELL.
 __device__ __forceinline__ size_t ell32_diag(const MeshDev &m, int n, int d) {
   return (size_t)(13 * 9 + d * 3 + d) * m.np + n;
+}
+
+// lift (bc.cuh) on double-float coordinates (ch + cl): w = e_r X with engineering shear, which only selects and
+// halves coordinates (exact).
+__device__ __forceinline__ void lift_df(const float (&ch)[3], const float (&cl)[3], int r, float (&wh)[3],
+                                        float (&wl)[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) wh[d] = wl[d] = 0.f;
+  if (r < 3) {
+    wh[r] = ch[r];
+    wl[r] = cl[r];
+  } else {
+    const int a = (r == 5) ? 1 : 0, b = (r == 3) ? 1 : 2;
+    wh[a] = 0.5f * ch[b];
+    wl[a] = 0.5f * cl[b];
+    wh[b] = 0.5f * ch[a];
+    wl[b] = 0.5f * cl[a];
+  }
 }
 
 }  // namespace
@@ -292,60 +312,86 @@ __global__ void k_add_du32(int nndim, const Inst *insts, const int *list) {
 // ---------------------------------------------------------------------------------------------------
 // Six right-hand sides of the implicit ctan.  The vectors are component-major, V[c6(i, d, np) + n].
 
-// f_i = -K_IB w_i on interior rows (FP64 accumulation of the FP32 tangent), 0 on boundary rows; x_i = 0.
-__global__ void __launch_bounds__(kNodeBlock) k_t6_rhs(MeshDev m, const Inst *insts, const int *list) {
+// X = 0, F = 0 and the Jacobi inverse of the tangent (boundary rows: identity rows) on every node; the right-hand
+// sides of the interior nodes next to the boundary follow (k_t6_rhs_near).
+__global__ void __launch_bounds__(kNodeBlock) k_t6_clear(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  if (n < m.nn) {
+  if (n >= m.nn) return;
+  int i, j, k;
+  const bool b = bnd(m, n, i, j, k);
+  const size_t np = m.np;
+#pragma unroll
+  for (int c = 0; c < 18; ++c) {
+    const size_t idx = (size_t)c * np + n;
+    I.F6h[idx] = 0.f;
+    I.F6l[idx] = 0.f;
+    I.X6h[idx] = 0.f;
+    I.X6l[idx] = 0.f;
+  }
+  float *__restrict__ kinv = I.kinv32;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) kinv[n * 3 + d] = b ? 1.0f : 1.0f / I.vals32[ell32_diag(m, n, d)];
+}
+
+// f_i = -K_IB w_i in double-float arithmetic on the interior nodes that have boundary neighbours -- the only
+// nonzero rows -- one thread per node of the list `near`; ||f_i||.  The boundary coordinates are split into float
+// pairs once per neighbour; the lift of a unit strain only selects and halves them (exact).
+__global__ void __launch_bounds__(kNodeBlock) k_t6_rhs_near(MeshDev m, const int *near, int nnear, const Inst *insts,
+                                                            const int *list) {
+  const Inst &I = insts[list[blockIdx.y]];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (t < nnear) {
+    const int n = near[t];
     int i, j, k;
-    const bool b = bnd(m, n, i, j, k);
+    bnd(m, n, i, j, k);
     const size_t np = m.np;
-    double f[6][3];
+    float fh[6][3], fl[6][3];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) f[r][0] = f[r][1] = f[r][2] = 0.0;
-    if (!b) {
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) fh[r][d] = fl[r][d] = 0.f;
 #pragma unroll 1
-      for (int s = 0; s < 27; ++s) {
-        const int nb = nb_of(m, n, s);
-        int bi, bj, bk;
-        if (!bnd(m, nb, bi, bj, bk)) continue;
-        double c[3];
-        bc_coords(m, bi, bj, bk, c);
-        double Kb[9];
-        ell32_block(m, I.vals32, n, s, Kb);
+    for (int s = 0; s < 27; ++s) {
+      const int bi = i + s % 3 - 1, bj = j + (s / 3) % 3 - 1, bk = k + s / 9 - 1;
+      if (!(bi == 0 || bj == 0 || bk == 0 || bi == m.nx - 1 || bj == m.ny - 1 || bk == m.nz - 1)) continue;
+      double c[3];
+      bc_coords(m, bi, bj, bk, c);
+      float ch[3], cl[3];
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-          double w[3];
-          lift(c, r, w);
+      for (int d = 0; d < 3; ++d) df_split(c[d], ch[d], cl[d]);
+      float Kb[9];
+      ell32_block(m, I.vals32, n, s, Kb);
 #pragma unroll
-          for (int fi = 0; fi < 3; ++fi) f[r][fi] -= Kb[fi * 3 + 0] * w[0] + Kb[fi * 3 + 1] * w[1] + Kb[fi * 3 + 2] * w[2];
-        }
+      for (int r = 0; r < 6; ++r) {
+        float wh[3], wl[3];
+        lift_df(ch, cl, r, wh, wl);
+#pragma unroll
+        for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+          for (int fj = 0; fj < 3; ++fj) df_sub_prod(fh[r][fi], fl[r][fi], Kb[fi * 3 + fj], wh[fj], wl[fj]);
       }
     }
-    double *__restrict__ F6 = I.F6;
-    double *__restrict__ X6 = I.X6;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const size_t idx = c6(r, d, np) + n;
-        F6[idx] = f[r][d];
-        X6[idx] = 0.0;
-        acc[r] += f[r][d] * f[r][d];
+        float h, l;
+        two_sum(fh[r][d], fl[r][d], h, l);
+        I.F6h[idx] = h;
+        I.F6l[idx] = l;
+        acc[r] = fmaf(h, h, acc[r]);
       }
-    // Jacobi inverse of the tangent for the 6-RHS CG (boundary rows are identity rows)
-    float *__restrict__ kinv = I.kinv32;
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      kinv[n * 3 + d] = b ? 1.0f : 1.0f / I.vals32[ell32_diag(m, n, d)];
   }
   double tot[6];
-  if (grid_sum<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
+  if (grid_sum_f<6>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0)
     for (int r = 0; r < 6; ++r) I.out->f6[r] = sqrt(tot[r]);
 }
 
-// Refinement residual RF = F - K X (FP64 accumulation), start of a 6-RHS CG on it:
+// Refinement residual RF = F - K X in double-float arithmetic (FP32 operations only: K is FP32, F and X are
+// double-float pairs; about 48 bits, enough for a 1e-9 relative residual), start of a 6-RHS CG on it:
 // R = RF (FP32), D = 0, Z = kinv R, P = Z; the last block initialises the six CG states.  x_zero: X is
 // still 0 (the first sweep), RF = F without the product.
 // mg as in k_cg32_setup.
@@ -353,19 +399,23 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
                                                             int x_zero, int mg) {
   const Inst &I = insts[list[blockIdx.y]];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[18];
+  float acc[18];
 #pragma unroll
-  for (int q = 0; q < 18; ++q) acc[q] = 0.0;  // [0,6): r.z  [6,12): z.z  [12,18): |RF|^2
+  for (int q = 0; q < 18; ++q) acc[q] = 0.f;  // [0,6): r.z  [6,12): z.z  [12,18): |RF|^2
   if (n < m.nn) {
     int i, j, k;
     const bool b = bnd(m, n, i, j, k);
     const size_t np = m.np;
-    const double *__restrict__ X6 = I.X6;
-    double rf[6][3];
+    const float *__restrict__ Xh = I.X6h;
+    const float *__restrict__ Xl = I.X6l;
+    float rh[6][3], rl[6][3];
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-      for (int d = 0; d < 3; ++d) rf[r][d] = b ? 0.0 : I.F6[c6(r, d, np) + n];
+      for (int d = 0; d < 3; ++d) {
+        rh[r][d] = b ? 0.f : I.F6h[c6(r, d, np) + n];
+        rl[r][d] = b ? 0.f : I.F6l[c6(r, d, np) + n];
+      }
     float kd[3], ksm[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -376,13 +426,20 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
 #pragma unroll 1
       for (int s = 0; s < 27; ++s) {
         const int nb = nb_of(m, n, s);
-        double Kb[9];
+        float Kb[9];
         ell32_block(m, I.vals32, n, s, Kb);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
-          const double x0 = X6[c6(r, 0, np) + nb], x1 = X6[c6(r, 1, np) + nb], x2 = X6[c6(r, 2, np) + nb];
+          float xh[3], xl[3];
 #pragma unroll
-          for (int fi = 0; fi < 3; ++fi) rf[r][fi] -= Kb[fi * 3] * x0 + Kb[fi * 3 + 1] * x1 + Kb[fi * 3 + 2] * x2;
+          for (int d = 0; d < 3; ++d) {
+            xh[d] = Xh[c6(r, d, np) + nb];
+            xl[d] = Xl[c6(r, d, np) + nb];
+          }
+#pragma unroll
+          for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+            for (int fj = 0; fj < 3; ++fj) df_sub_prod(rh[r][fi], rl[r][fi], Kb[fi * 3 + fj], xh[fj], xl[fj]);
         }
       }
     }
@@ -395,20 +452,20 @@ __global__ void __launch_bounds__(kNodeBlock) k_t6_residual(MeshDev m, const Ins
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const size_t idx = c6(r, d, np) + n;
-        const float rr = (float)rf[r][d];
+        const float rr = __fadd_rn(rh[r][d], rl[r][d]);
         const float zj = kd[d] * rr;
         const float z = ksm[d] * rr;
         R6[idx] = rr;
         Z6[idx] = z;
         P6[idx] = z;
         D6[idx] = 0.0f;
-        acc[r] += (double)rr * (double)z;
-        acc[6 + r] += (double)zj * (double)zj;
-        acc[12 + r] += rf[r][d] * rf[r][d];
+        acc[r] = fmaf(rr, z, acc[r]);
+        acc[6 + r] = fmaf(zj, zj, acc[6 + r]);
+        acc[12 + r] = fmaf(rr, rr, acc[12 + r]);
       }
   }
   double tot[18];
-  if (grid_sum<18>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
+  if (grid_sum_f<18>(acc, I.red, I.ticket, gridDim.x, tot) && threadIdx.x == 0) {
     Cg6State *c = I.cg6;
     c->its = 0;
     int all = 1;
@@ -634,29 +691,37 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg6_pupdate(MeshDev m, const Ins
   }
 }
 
-// X += D (FP64 accumulation of the FP32 correction), one thread per node.
+// X += D (double-float accumulation of the FP32 correction), one thread per node.
 __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
   const Inst &I = insts[list[blockIdx.y]];
   const size_t np = m.np;
-  double *__restrict__ X6 = I.X6;
+  float *__restrict__ Xh = I.X6h;
+  float *__restrict__ Xl = I.X6l;
   const float *__restrict__ D6 = I.D6;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < m.nn; n += gridDim.x * blockDim.x)
 #pragma unroll
-    for (int c = 0; c < 18; ++c) X6[(size_t)c * np + n] += (double)D6[(size_t)c * np + n];
+    for (int c = 0; c < 18; ++c) {
+      const size_t idx = (size_t)c * np + n;
+      float h = Xh[idx], l = Xl[idx];
+      df_add(h, l, D6[idx]);
+      Xh[idx] = h;
+      Xl[idx] = l;
+    }
 }
 
 // ctan in the energy form, element by element (FP32 Jacobian assembled by node gather: elastic and damage
 // phases, a symmetric tangent).  With v_i = w_i + x_i the tangent field of unit strain i (w_i the boundary lift,
-// x_i the interior solution X6),
+// x_i the interior solution X6h + X6l),
 //   ctan[k][i] = (1/V) sum_e sum_g wg eps(v_k)^T C_g eps(v_i),
 // C_g the Gauss-point tangent: the phase's elastic C, or for damage a C + c s s^T from the tangent terms the FP64
 // residual wrote.  The form is stationary at the exact x, so its error is quadratic in the error of x (the FP32
 // solves and the FP32 rounding of the assembled tangent they used).  Summing element energies also avoids the
 // cancellation of v^T (K v) over assembled rows -- K v nearly vanishes on interior rows -- whose first-order
 // rounding with FP32 rows reached 1e-5 on 60^3 RVEs.  Block: kEnElems elements x 8 threads.  Thread a of an
-// element loads node a's six fields in FP64 and keeps their differences from node 0 in FP32 (the strains
-// need only differences: sum_a dN_a = 0); then, as Gauss point g, it forms the six strains, the tangent
-// products and the 21 energies.  FP32 per element, FP64 across elements.
+// element loads node a's six fields as double-float pairs (boundary nodes: the lift of the split coordinates)
+// and keeps their differences from node 0 in FP32 (the strains need only differences: sum_a dN_a = 0); then,
+// as Gauss point g, it forms the six strains, the tangent products and the 21 energies.  FP32 per element,
+// FP64 across elements.
 constexpr int kEnElems = 32;
 constexpr int kEnStride = 7 * 18 + 1;  // differences of nodes 1..7, 6 fields x 3; odd stride
 
@@ -670,9 +735,9 @@ __global__ void __launch_bounds__(kEnElems * 8) k_ctan_energy(MeshDev m, Mats ma
   const int e = blockIdx.x * kEnElems + el;
   const bool valid = e < m.nelem;
   const size_t np = m.np;
-  double v[18];
+  float vh[18], vl[18];  // the node's six fields as double-float pairs
 #pragma unroll
-  for (int q = 0; q < 18; ++q) v[q] = 0.0;
+  for (int q = 0; q < 18; ++q) vh[q] = vl[q] = 0.f;
   if (valid) {
     const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
     const int n = (ez + c_corner6[sub][2]) * m.nxny + (ey + c_corner6[sub][1]) * m.nx + ex + c_corner6[sub][0];
@@ -680,20 +745,35 @@ __global__ void __launch_bounds__(kEnElems * 8) k_ctan_energy(MeshDev m, Mats ma
     if (bnd(m, n, bi, bj, bk)) {
       double X[3];
       bc_coords(m, bi, bj, bk, X);
+      float ch[3], cl[3];
 #pragma unroll
-      for (int r = 0; r < 6; ++r) lift(X, r, &v[r * 3]);
+      for (int d = 0; d < 3; ++d) df_split(X[d], ch[d], cl[d]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        float wh[3], wl[3];
+        lift_df(ch, cl, r, wh, wl);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          vh[r * 3 + d] = wh[d];
+          vl[r * 3 + d] = wl[d];
+        }
+      }
     } else {
 #pragma unroll
       for (int r = 0; r < 6; ++r)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) v[r * 3 + d] = I.X6[c6(r, d, np) + n];
+        for (int d = 0; d < 3; ++d) {
+          vh[r * 3 + d] = I.X6h[c6(r, d, np) + n];
+          vl[r * 3 + d] = I.X6l[c6(r, d, np) + n];
+        }
     }
   }
   const int lane0 = (threadIdx.x & 31) & ~7;  // node 0 of this element, in the same warp
 #pragma unroll
   for (int q = 0; q < 18; ++q) {
-    const double v0 = __shfl_sync(0xffffffffu, v[q], lane0);
-    if (sub > 0) dv[el * kEnStride + (sub - 1) * 18 + q] = (float)(v[q] - v0);
+    const float h0 = __shfl_sync(0xffffffffu, vh[q], lane0), l0 = __shfl_sync(0xffffffffu, vl[q], lane0);
+    if (sub > 0)
+      dv[el * kEnStride + (sub - 1) * 18 + q] = __fadd_rn(__fsub_rn(vh[q], h0), __fsub_rn(vl[q], l0));
   }
   __syncthreads();
   float acc[21];
@@ -823,8 +903,9 @@ __global__ void __launch_bounds__(128) k_ctan_avg(MeshDev m, Mats mats, const in
       double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
-        double ux = I.X6[c6(r, 0, np) + nodes[a]], uy = I.X6[c6(r, 1, np) + nodes[a]],
-               uz = I.X6[c6(r, 2, np) + nodes[a]];
+        const size_t i0 = c6(r, 0, np) + nodes[a], i1 = c6(r, 1, np) + nodes[a], i2 = c6(r, 2, np) + nodes[a];
+        double ux = (double)I.X6h[i0] + (double)I.X6l[i0], uy = (double)I.X6h[i1] + (double)I.X6l[i1],
+               uz = (double)I.X6h[i2] + (double)I.X6l[i2];
         if (nb_bnd[a]) {
           double w[3];
           lift(cc[a], r, w);
@@ -958,9 +1039,15 @@ int mgb_launch_axpy_du32(const MeshDev *m, double *u, const float *du, double a,
   return (int)cudaGetLastError();
 }
 
-int mgb_launch_t6_rhs(const MeshDev *m, const Inst *insts, const int *list, int nlist, cudaStream_t s) {
+int mgb_launch_t6_rhs(const MeshDev *m, const int *near, int nnear, const Inst *insts, const int *list, int nlist,
+                      cudaStream_t s) {
   if (nlist <= 0) return 0;
-  k_t6_rhs<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  k_t6_clear<<<dim3(cdiv(m->nn, kNodeBlock), nlist), kNodeBlock, 0, s>>>(*m, insts, list);
+  const int e = (int)cudaGetLastError();
+  if (e) return e;
+  // at least one block, which publishes ||f_i|| = 0 when no interior node touches the boundary
+  const int nb = nnear > 0 ? cdiv(nnear, kNodeBlock) : 1;
+  k_t6_rhs_near<<<dim3(nb, nlist), kNodeBlock, 0, s>>>(*m, near, nnear, insts, list);
   return (int)cudaGetLastError();
 }
 

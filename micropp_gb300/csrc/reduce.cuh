@@ -13,6 +13,7 @@
 #pragma once
 
 #include "device.cuh"
+#include "df.cuh"
 
 namespace mgb {
 
@@ -49,25 +50,30 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sh) {
   }
 }
 
-// Block sum of FP32 per-thread partials: FP32 within each warp, FP64 across the warps.  The FP64 result is
-// valid in thread 0.  `sh` holds 32*K doubles.
+// Block sum of FP32 per-thread partials: FP32 within each warp, FP64 across the warps, value k by thread k
+// (one FP64 add per warp and value, issued by K lanes together rather than by one thread in turn).  The FP64
+// result is valid in thread 0.  `sh` holds 32*K doubles: the warp sums as floats in its first half, the block
+// sums as doubles in its second.
 template <int K>
 __device__ __forceinline__ void block_sum_f(float (&v)[K], double (&out)[K], double *sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  float *shf = reinterpret_cast<float *>(sh);
+  double *shd = sh + 16 * K;
   warp_sum<K>(v);
   __syncthreads();
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < K; ++k) sh[wid * K + k] = (double)v[k];
+    for (int k = 0; k < K; ++k) shf[wid * K + k] = v[k];
   __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double a = sh[k];
-      for (int w = 1; w < nw; ++w) a += sh[w * K + k];
-      out[k] = a;
-    }
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double a = (double)shf[k];
+    for (int w = 1; w < nw; ++w) a += (double)shf[w * K + k];
+    shd[k] = a;
   }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = shd[k];
 }
 
 // Second half of a grid reduction: `v` holds the block's sums in thread 0.  Returns true in the last block,
@@ -122,6 +128,37 @@ __device__ __forceinline__ bool grid_sum_f(float (&v)[K], double *red, unsigned 
   double bs[K];
   block_sum_f<K>(v, bs, sh);
   __syncthreads();  // sh is reused by the last block
+  return grid_finish<K>(bs, sh, red, ticket, nblocks, total);
+}
+
+// Grid reduction of double-float per-thread values: double-float within a warp (FP32 operations), FP64 from
+// the warp sums up (value k by thread k, as block_sum_f).
+template <int K>
+__device__ __forceinline__ bool grid_sum_df(dfl (&v)[K], double *red, unsigned int *ticket, int nblocks,
+                                            double (&total)[K]) {
+  __shared__ double sh[32 * K];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const dfl u{__shfl_down_sync(0xffffffffu, v[k].h, o), __shfl_down_sync(0xffffffffu, v[k].l, o)};
+      v[k] = v[k] + u;
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[wid * K + k] = df_to_double(v[k]);
+  __syncthreads();
+  __shared__ double shd[K];
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double a = sh[k];
+    for (int w = 1; w < nw; ++w) a += sh[w * K + k];
+    shd[k] = a;
+  }
+  __syncthreads();
+  double bs[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) bs[k] = shd[k];
   return grid_finish<K>(bs, sh, red, ticket, nblocks, total);
 }
 
