@@ -91,6 +91,8 @@ struct InstOut {
 // operator is the Galerkin product P^T A P in the fine grid's stencil ELL layout; its vectors hold up to 6
 // right-hand sides component-major, v[(r * 3 + d) * np_l + n], and are zero on boundary nodes.
 constexpr int kMgMaxLevels = 8;
+// A coarsest multigrid level of at most this many nodes runs its Jacobi sweeps in one block per instance.
+constexpr int kMgCoarseNodes = 1024;
 
 struct MgLevel {
   float *vals;             // 243 * np_l (level >= 1)

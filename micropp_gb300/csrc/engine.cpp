@@ -1055,11 +1055,18 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
                                         stream_),
                  "multigrid restriction");
   }
-  for (int k = 0; k < kMgCoarsePairs; ++k) {
-    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 0, 1, 1.0f, stream_),
-                 "multigrid coarse sweep");
-    check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 1, 0, 1.0f, stream_),
-                 "multigrid coarse sweep");
+  const bool one_block = mg_mesh_[L - 1].nn <= kMgCoarseNodes;
+  if (one_block) {
+    check_launch(mgb_launch_mg_coarse_sweeps(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, kMgCoarsePairs,
+                                             1.0f, stream_),
+                 "multigrid coarse sweeps");
+  } else {
+    for (int k = 0; k < kMgCoarsePairs; ++k) {
+      check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 0, 1, 1.0f, stream_),
+                   "multigrid coarse sweep");
+      check_launch(mgb_launch_mg_jacobi(&mg_mesh_[L - 1], d_insts_, d_list_, nlist, nr, L - 1, 1, 0, 1.0f, stream_),
+                   "multigrid coarse sweep");
+    }
   }
   for (int l = L - 2; l >= 0; --l) {
     check_launch(mgb_launch_mg_prolong(&mg_mesh_[l], &mg_mesh_[l + 1], d_insts_, d_list_, nlist, nr, l, stream_),
@@ -1074,7 +1081,7 @@ void Engine::mg_vcycle(int nr, int nlist, bool setup, int block) {
                                    stream_),
                "multigrid level-0 post-smoother");
   timer_end(fine);
-  launches_ += 2 * (L - 1) + 2 * kMgCoarsePairs + (L - 1) + (L - 2) + 1;
+  launches_ += 2 * (L - 1) + (one_block ? 1 : 2 * kMgCoarsePairs) + (L - 1) + (L - 2) + 1;
 }
 
 // Implicit ctan of the listed slots at their current u with their vars_old: assemble the FP32 tangent, form

@@ -108,6 +108,10 @@ int mgb_launch_mg_prolong(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const 
                           int nlist, int nr, int lf, cudaStream_t s);
 int mgb_launch_mg_jacobi(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
                          int src, int dst, float omega, cudaStream_t s);
+// `pairs` pairs of Jacobi sweeps x -> y -> x on level l >= 1 of at most kMgCoarseNodes nodes, in one launch
+// (one block per instance); the same result as 2 x pairs mgb_launch_mg_jacobi calls.
+int mgb_launch_mg_coarse_sweeps(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr,
+                                int l, int pairs, float omega, cudaStream_t s);
 // block: threads per block of the 6-RHS form (64, 128 or 256; two nodes per thread), as mgb_launch_mg_resid.
 int mgb_launch_mg_post0(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr,
                         float omega, int setup, int block, int half, cudaStream_t s);

@@ -42,6 +42,7 @@ namespace mgb {
 namespace {
 
 constexpr int kMgBlock = 128;
+constexpr int kMgCoarseBlock = 256;
 
 // The FP16 copy of the level-0 operator (MICROPP3_PRECOND_MG_HALF): scale16 x the FP32 values, streamed by the
 // two level-0 smoothing passes; their sums are rescaled by inv16, an exact power of two.
@@ -379,17 +380,38 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_prolong(MeshDev mf, MeshDev mc,
     for (int d = 0; d < 3; ++d) f.t[vix<RMF>(r, d, n, npf)] = acc[r * 3 + d];
 }
 
-// out = in + w D^-1 (b - A in) on level l >= 1 (zero on boundary nodes); in/out select x, y or t.
+// apply_node (component-major vectors) for an x that the same kernel wrote before a barrier: x is read through
+// L2 (ld.global.cg), never through the read-only path.  The same products in the same order.
 template <int NR>
-__global__ void __launch_bounds__(kMgBlock) k_mg_jacobi(MeshDev m, const Inst *insts, const int *list, int l,
-                                                        int src, int dst, float omega) {
-  const Inst &I = insts[list[blockIdx.y]];
-  if (inst_done<NR>(I)) return;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= m.nn) return;
-  const LvView v = view<NR>(I, l);
-  const float *__restrict__ in = pick(v, src);
-  float *__restrict__ out = pick(v, dst);
+__device__ __forceinline__ void apply_node_cg(const MeshDev &m, const float *__restrict__ vals, const float *x, int n,
+                                              float (&y)[NR * 3]) {
+  const size_t np = m.np;
+#pragma unroll
+  for (int c = 0; c < NR * 3; ++c) y[c] = 0.f;
+#pragma unroll 3
+  for (int s = 0; s < 27; ++s) {
+    const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
+    float K[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) K[q] = __ldg(vals + (size_t)(s * 9 + q) * np + n);
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      float xv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xv[d] = __ldcg(x + vix<false>(r, d, nb, np));
+#pragma unroll
+      for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj) y[r * 3 + fi] = fmaf(K[fi * 3 + fj], xv[fj], y[r * 3 + fi]);
+    }
+  }
+}
+
+// out = in + w D^-1 (b - A in) at node n of level l >= 1 (zero on boundary nodes).  CG: `in` was written by the
+// same kernel (k_mg_coarse_sweeps) and is read through L2.
+template <int NR, bool CG>
+__device__ __forceinline__ void jacobi_node(const MeshDev &m, const LvView &v, const float *in, float *out, int n,
+                                            float omega) {
   const size_t np = m.np;
   int i, j, k;
   if (on_boundary(m, n, i, j, k)) {
@@ -398,14 +420,47 @@ __global__ void __launch_bounds__(kMgBlock) k_mg_jacobi(MeshDev m, const Inst *i
     return;
   }
   float y[NR * 3];
-  apply_node<NR, false, false>(m, v.vals, in, n, y);
+  if constexpr (CG)
+    apply_node_cg<NR>(m, v.vals, in, n, y);
+  else
+    apply_node<NR, false, false>(m, v.vals, in, n, y);
 #pragma unroll
   for (int r = 0; r < NR; ++r)
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const size_t q = (size_t)(r * 3 + d) * np + n;
-      out[q] = fmaf(omega * v.kinv[(size_t)n * 3 + d], v.b[q] - y[r * 3 + d], in[q]);
+      const float xin = CG ? __ldcg(in + q) : in[q];
+      out[q] = fmaf(omega * v.kinv[(size_t)n * 3 + d], v.b[q] - y[r * 3 + d], xin);
     }
+}
+
+// One Jacobi sweep on level l >= 1; in/out select x, y or t.
+template <int NR>
+__global__ void __launch_bounds__(kMgBlock) k_mg_jacobi(MeshDev m, const Inst *insts, const int *list, int l,
+                                                        int src, int dst, float omega) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const LvView v = view<NR>(I, l);
+  jacobi_node<NR, false>(m, v, pick(v, src), pick(v, dst), n, omega);
+}
+
+// The coarsest level's Jacobi sweeps in one block per instance: `pairs` pairs x -> y -> x, each sweep the
+// arithmetic of k_mg_jacobi (so the result is the same bit for bit), the block's barrier between sweeps.  For
+// levels of at most kMgCoarseNodes nodes, where a launch per sweep costs more than the sweep.
+template <int NR>
+__global__ void __launch_bounds__(kMgCoarseBlock) k_mg_coarse_sweeps(MeshDev m, const Inst *insts, const int *list,
+                                                                     int l, int pairs, float omega) {
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const LvView v = view<NR>(I, l);
+  for (int p = 0; p < 2 * pairs; ++p) {
+    const float *in = (p & 1) ? v.y : v.x;
+    float *out = (p & 1) ? v.x : v.y;
+    for (int n = threadIdx.x; n < m.nn; n += blockDim.x) jacobi_node<NR, true>(m, v, in, out, n, omega);
+    __syncthreads();
+  }
 }
 
 // The CG scalars after the level-0 post-smoother (last block of the instance, thread 0): setup sets rz, an
@@ -738,6 +793,18 @@ int mgb_launch_mg_prolong(const MeshDev *mf, const MeshDev *mc, const Inst *inst
   } else {
     k_mg_prolong<6, false><<<g, kMgBlock, 0, s>>>(*mf, *mc, insts, list, lf);
   }
+  return (int)cudaGetLastError();
+}
+
+int mgb_launch_mg_coarse_sweeps(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l,
+                                int pairs, float omega, cudaStream_t s) {
+  if (nlist <= 0 || pairs <= 0) return 0;
+  if (l < 1 || m->nn > kMgCoarseNodes) return (int)cudaErrorInvalidValue;
+  const dim3 g(1, nlist);
+  if (nr == 1)
+    k_mg_coarse_sweeps<1><<<g, kMgCoarseBlock, 0, s>>>(*m, insts, list, l, pairs, omega);
+  else
+    k_mg_coarse_sweeps<6><<<g, kMgCoarseBlock, 0, s>>>(*m, insts, list, l, pairs, omega);
   return (int)cudaGetLastError();
 }
 
