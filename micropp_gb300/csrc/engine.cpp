@@ -964,7 +964,7 @@ void Engine::assemble32(int nlist) {
     timer_begin(t_asm_, (double)nlist * (4.0 * kEllPerNode * mesh_.np + 4.0 * 64.0 * mesh_.nelem));
     launches_ += 1;
     check_launch(mgb_launch_assembly_gather32(&mesh_, &mats_, d_etype_, d_k0g32_, d_ke32_, d_dsh32_, d_insts_,
-                                              d_list_, nlist, stream_),
+                                              d_list_, nlist, kMgOmega, kMgSafe, mg_ ? 1 : 0, stream_),
                  "assembly (FP32 gather)");
   } else {
     timer_begin(t_asm_, (double)nlist * (4.0 * kEllPerNode * mesh_.np + 8.0 * nndim() + 8.0 * nvars()));
@@ -973,17 +973,18 @@ void Engine::assemble32(int nlist) {
                  "assembly (FP32)");
   }
   timer_end(t_asm_);
-  if (mg_) mg_rap(nlist);
+  if (mg_) mg_rap(nlist, gather32_);
 }
 
 // Galerkin operators P^T A P of every coarse level, finest first, each as three 1-D steps (x, y, z) through
-// the intermediate operators mid1 and mid2, and the safeguarded smoother diagonal of every level.  Algorithmic
-// bytes: each step reads its input operator and writes its output once; each level's diagonal reads its operator.
-void Engine::mg_rap(int nlist) {
+// the intermediate operators mid1 and mid2, and the safeguarded smoother diagonal of every level (of level 0 only
+// when the assembly did not write it: sdiag0_done).  Algorithmic bytes: each step reads its input operator and
+// writes its output once; each diagonal pass reads its operator.
+void Engine::mg_rap(int nlist, bool sdiag0_done) {
   double bytes = 0.0;
   for (size_t l = 0; l < mg_mesh_.size(); ++l) {
     const MeshDev &f = mg_mesh_[l];
-    bytes += 4.0 * kEllPerNode * (double)f.np;
+    if (l > 0 || !sdiag0_done) bytes += 4.0 * kEllPerNode * (double)f.np;
     if (l + 1 < mg_mesh_.size()) {
       const MeshDev &c = mg_mesh_[l + 1];
       const double n1 = grid_of(c.nx, f.ny, f.nz).np, n2 = grid_of(c.nx, c.ny, f.nz).np;
@@ -991,9 +992,11 @@ void Engine::mg_rap(int nlist) {
     }
   }
   timer_begin(t_rap_, nlist * bytes);
-  launches_ += 1;
-  check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
-               "multigrid smoother diagonal");
+  if (!sdiag0_done) {
+    launches_ += 1;
+    check_launch(mgb_launch_mg_sdiag(&mg_mesh_[0], d_insts_, d_list_, nlist, 0, kMgOmega, kMgSafe, stream_),
+                 "multigrid smoother diagonal");
+  }
   if (mg_half_) {
     launches_ += 1;
     check_launch(mgb_launch_mg_half0(&mg_mesh_[0], d_insts_, d_list_, nlist, stream_), "multigrid FP16 operator");

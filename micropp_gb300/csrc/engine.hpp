@@ -195,7 +195,7 @@ class Engine {
   int bicg_solve(bool transpose, double *x);
   // Multigrid (engine.cpp): Galerkin operators of the listed slots after an FP32 assembly; one V-cycle of the
   // 1- or 6-RHS CG of the listed slots, ending with the level-0 post-smoother (setup: start of a solve).
-  void mg_rap(int nlist);
+  void mg_rap(int nlist, bool sdiag0_done);
   void mg_vcycle(int nr, int nlist, bool setup, int block);
   // Algorithmic bytes of one V-cycle per instance: its two level-0 operator passes, and the rest.
   double mg_fine_bytes(int nr) const;

@@ -783,7 +783,8 @@ __device__ __forceinline__ void asm_store(const float (&acc)[8][9], float *row) 
 __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_gather32(MeshDev m, Mats mats, const int8_t *etype,
                                                               const float *k0g, const float *kesum,
                                                               const float *dsh_g, const Inst *insts,
-                                                              const int *list) {
+                                                              const int *list, float omega, float csafe,
+                                                              int sdiag) {
   __shared__ float rows[kAsmNodes * kAsmRow];
   __shared__ float dsh[8 * 24];
   for (int t = threadIdx.x; t < kAsmNodes * kAsmRow; t += blockDim.x) rows[t] = 0.f;
@@ -817,6 +818,27 @@ __global__ void __launch_bounds__(kAsmNodes * 8) k_asm_gather32(MeshDev m, Mats 
   float *__restrict__ vals = I.vals32;
   const size_t np = m.np;
   for (int E = w; E < kEllPerNode; E += 8) vals[(size_t)E * np + (size_t)blockIdx.x * kAsmNodes + lane] = rows[lane * kAsmRow + E];
+  // sdiag: the multigrid's level-0 smoother diagonal from the rows in shared memory, warp fi for row fi of each
+  // node: 1 / max(a_ii / omega, csafe sum_j |a_ij|) over interior columns, the sums in k_mg_sdiag's order (so
+  // the same values bit for bit); boundary rows 1.
+  if (sdiag && w < 3 && valid) {
+    const int fi = w;
+    float *__restrict__ kinv = I.mg->lv[0].kinv;
+    if (i == 0 || j == 0 || k == 0 || i == m.nx - 1 || j == m.ny - 1 || k == m.nz - 1) {
+      kinv[(size_t)n * 3 + fi] = 1.f;
+    } else {
+      const float *row = &rows[lane * kAsmRow];
+      float l1 = 0.f;
+#pragma unroll
+      for (int s = 0; s < 27; ++s) {
+        const int bi = i + s % 3 - 1, bj = j + (s / 3) % 3 - 1, bk = k + s / 9 - 1;
+        if (bi == 0 || bj == 0 || bk == 0 || bi == m.nx - 1 || bj == m.ny - 1 || bk == m.nz - 1) continue;
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj) l1 += fabsf(row[s * 9 + fi * 3 + fj]);
+      }
+      kinv[(size_t)n * 3 + fi] = 1.f / fmaxf(row[13 * 9 + fi * 4] / omega, csafe * l1);
+    }
+  }
 }
 
 // Zero the ELL values of the listed instances (ell_set_zero_mat, ell-common.cpp:200).
@@ -983,10 +1005,10 @@ int mgb_launch_assembly32(const MeshDev *m, const Mats *mats, const int8_t *etyp
 
 int mgb_launch_assembly_gather32(const MeshDev *m, const Mats *mats, const int8_t *etype, const float *k0g,
                               const float *kesum, const float *dsh32, const Inst *insts, const int *list, int nlist,
-                              cudaStream_t s) {
+                              float omega, float csafe, int sdiag, cudaStream_t s) {
   if (nlist <= 0) return 0;
   k_asm_gather32<<<dim3(cdiv(m->np, kAsmNodes), nlist), kAsmNodes * 8, 0, s>>>(*m, *mats, etype, k0g, kesum, dsh32,
-                                                                             insts, list);
+                                                                             insts, list, omega, csafe, sdiag);
   return (int)cudaGetLastError();
 }
 

@@ -42,9 +42,10 @@ int mgb_launch_assembly32(const mgb::MeshDev *m, const mgb::Mats *mats, const in
                           const float *ke_phase, const mgb::Inst *insts, const int *list, int nlist, cudaStream_t s);
 // FP32 Jacobian by node gather (every phase elastic or damage): k0g = wg B_g^T C B_g per phase and Gauss
 // point [3][8][576], kesum = its sum over g per phase [3][576], dsh32 = the shape-function gradients [8][24].
+// sdiag = 1: also the multigrid's level-0 smoother diagonal, as mgb_launch_mg_sdiag(l = 0, omega, csafe).
 int mgb_launch_assembly_gather32(const mgb::MeshDev *m, const mgb::Mats *mats, const int8_t *etype, const float *k0g,
                               const float *kesum, const float *dsh32, const mgb::Inst *insts, const int *list,
-                              int nlist, cudaStream_t s);
+                              int nlist, float omega, float csafe, int sdiag, cudaStream_t s);
 // mg = 1: a V-cycle and mgb_launch_mg_post0 with setup = 1 follow.
 int mgb_launch_cg32_setup(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int mg,
                           cudaStream_t s);
