@@ -22,10 +22,11 @@ enum { MICROPP3_FE_LINEAR = 0, MICROPP3_FE_ONE_WAY = 1, MICROPP3_FE_FULL = 2, MI
 /* Arithmetic of the homogenization. */
 enum {
   MICROPP3_FP64 = 0,  /* the reference algorithm in FP64 throughout (drop-in parity form) */
-  MICROPP3_MIXED = 1  /* FP32 Jacobian and CG inside FP64 iterative refinement; FP64 residual and averages.
-                        * Newton starts from the previous solution moved with the strain increment and has a
-                        * line search; its FP32 CG stops at no less than 1e-6 relative (the FP64 residual
-                        * decides convergence, to nr_rel_tol). */
+  MICROPP3_MIXED = 1  /* FP32 Jacobian and CG inside FP64 iterative refinement; FP64-accurate residual and
+                        * averages (double-float arithmetic on the FP32 pipe, about 46 bits, for elastic and
+                        * damage phases; FP64 with a J2 phase).  Newton starts from the previous solution moved
+                        * with the strain increment and has a line search; its FP32 CG stops at no less than
+                        * 1e-6 relative (the FP64-accurate residual decides convergence, to nr_rel_tol). */
 };
 
 /* How ctan is obtained for a nonlinear macro point. */

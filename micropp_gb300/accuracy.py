@@ -3,7 +3,7 @@
 The FP64 solution comes from the library's FP64 load-path solver (micropp3_path_forward): FP64 Newton with
 the exact consistent tangent of the laws (forward-mode dual numbers), BiCGSTAB corrections to 1e-12 and the
 Newton residual to 1e-11 of its initial value, absolute stop off -- a solver that shares no code with the fast
-form's FP32 Jacobian, FP32 CG and implicit ctan beyond the FP64 residual and the laws.  The path takes the
+form's FP32 Jacobian, FP32 CG, double-float residual and implicit ctan beyond the laws.  The path takes the
 previous macro step (history strain) and accepts it, then the step to the strain checked.  Its ctan is exact
 in FP64 too: for L = sigma_k of the last step, the reverse-mode pass (micropp3_path_vjp) gives
 dL/d(strain of the last step) = row k of ctan, since that strain reaches sigma only through the last step's
