@@ -1,4 +1,5 @@
-// fe_kernels.cu -- finite-element kernels of the FP64 homogenization path (sm_103a).
+// fe_kernels.cu -- finite-element kernels of the homogenization path (sm_103a): the FP64 form's residual and
+// colour-ordered assembly, the mixed form's double-float residual and FP32 assemblies, the history update.
 //
 // Every kernel runs over a batch: blockIdx.y indexes the list of active instances, blockIdx.x tiles the
 // nodes or elements of one RVE.  Summation orders follow the reference where a sum is local (Gauss points of
@@ -101,7 +102,8 @@ __global__ void k_copy(int n, const double *const *src, double *const *dst, cons
 // Element residual blocks be = sum_gp B^T sigma(B u_e, vars) wg (assembly.cpp:123-138), one thread per
 // element, plus the element's share of the volume average of sigma (average.cpp:57-82), reduced over the
 // grid into out.sig.  Each term is formed as (g sigma) wg, the reference's order: the FP64 form's iteration
-// counts match the reference's.  The mixed form uses k_elem_rhs_sf.
+// counts match the reference's.  The mixed form uses k_elem_rhs_df (elastic and damage phases) or
+// k_elem_rhs_sf (with a J2 phase).
 __global__ void __launch_bounds__(kElemBlock) k_elem_rhs(MeshDev m, Mats mats, const int8_t *etype,
                                                            const double *dsh_g, const Inst *insts,
                                                            const int *list) {
