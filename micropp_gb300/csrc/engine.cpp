@@ -155,6 +155,7 @@ Engine::Engine(const micropp3_config &cfg) {
   }
 
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  if (mg_) check_launch(mgb_mg_init_attributes(), "multigrid kernel attributes");
   check(cudaEventCreate(&ev0_), "event");
   check(cudaEventCreate(&ev1_), "event");
   d_etype_ = dalloc<int8_t>(mesh_.nelem, "elem_type");

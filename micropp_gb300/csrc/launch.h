@@ -110,7 +110,11 @@ int mgb_launch_mg_prolong(const mgb::MeshDev *mf, const mgb::MeshDev *mc, const 
 int mgb_launch_mg_jacobi(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr, int l,
                          int src, int dst, float omega, cudaStream_t s);
 // `pairs` pairs of Jacobi sweeps x -> y -> x on level l >= 1 of at most kMgCoarseNodes nodes, in one launch
-// (one block per instance); the same result as 2 x pairs mgb_launch_mg_jacobi calls.
+// (one block per instance, the level in shared memory when it fits); the same result as 2 x pairs
+// mgb_launch_mg_jacobi calls.  mgb_mg_init_attributes must have run on the device first.
+// The kernel attributes the multigrid launches need (the shared-memory size of the coarse sweeps), on the current
+// device; call before the first V-cycle and outside any stream capture.
+int mgb_mg_init_attributes();
 int mgb_launch_mg_coarse_sweeps(const mgb::MeshDev *m, const mgb::Inst *insts, const int *list, int nlist, int nr,
                                 int l, int pairs, float omega, cudaStream_t s);
 // block: threads per block of the 6-RHS form (64, 128 or 256; two nodes per thread), as mgb_launch_mg_resid.

@@ -43,6 +43,7 @@ namespace {
 
 constexpr int kMgBlock = 128;
 constexpr int kMgCoarseBlock = 256;
+constexpr int kMgCoarseSmem = 200 * 1024;  // shared memory of the shared-memory coarse sweeps, at most
 
 // The FP16 copy of the level-0 operator (MICROPP3_PRECOND_MG_HALF): scale16 x the FP32 values, streamed by the
 // two level-0 smoothing passes; their sums are rescaled by inv16, an exact power of two.
@@ -463,6 +464,73 @@ __global__ void __launch_bounds__(kMgCoarseBlock) k_mg_coarse_sweeps(MeshDev m, 
   }
 }
 
+// k_mg_coarse_sweeps with the level in shared memory: the operator (243 np floats), x, y, b (NR * 3 * np each)
+// and the inverse diagonal (3 np) are loaded once, every sweep reads them there, and x goes back at the end.
+// The products and sums are those of jacobi_node in the same order, so x is the same bit for bit.
+template <int NR>
+__global__ void __launch_bounds__(kMgCoarseBlock) k_mg_coarse_sweeps_smem(MeshDev m, const Inst *insts,
+                                                                          const int *list, int l, int pairs,
+                                                                          float omega) {
+  extern __shared__ float sm[];
+  const Inst &I = insts[list[blockIdx.y]];
+  if (inst_done<NR>(I)) return;
+  const LvView v = view<NR>(I, l);
+  const size_t np = m.np, nv = (size_t)NR * 3 * np;
+  float *A = sm, *xs = A + (size_t)kEllPerNode * np, *ys = xs + nv, *bs = ys + nv, *kd = bs + nv;
+  for (size_t t = threadIdx.x; t < (size_t)kEllPerNode * np; t += blockDim.x) A[t] = __ldg(v.vals + t);
+  for (size_t t = threadIdx.x; t < nv; t += blockDim.x) {
+    xs[t] = v.x[t];
+    ys[t] = 0.f;
+    bs[t] = v.b[t];
+  }
+  for (size_t t = threadIdx.x; t < (size_t)3 * m.nn; t += blockDim.x) kd[t] = v.kinv[t];
+  __syncthreads();
+  for (int p = 0; p < 2 * pairs; ++p) {
+    const float *in = (p & 1) ? ys : xs;
+    float *out = (p & 1) ? xs : ys;
+    for (int n = threadIdx.x; n < m.nn; n += blockDim.x) {
+      int i, j, k;
+      if (on_boundary(m, n, i, j, k)) {
+#pragma unroll
+        for (int c = 0; c < NR * 3; ++c) out[(size_t)c * np + n] = 0.f;
+        continue;
+      }
+      float y[NR * 3];
+#pragma unroll
+      for (int c = 0; c < NR * 3; ++c) y[c] = 0.f;
+#pragma unroll 3
+      for (int s = 0; s < 27; ++s) {
+        const int nb = n + (s / 9 - 1) * m.nxny + ((s / 3) % 3 - 1) * m.nx + (s % 3 - 1);
+        float K[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) K[q] = A[(size_t)(s * 9 + q) * np + n];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+          float xv[3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) xv[d] = in[(size_t)(r * 3 + d) * np + nb];
+#pragma unroll
+          for (int fi = 0; fi < 3; ++fi)
+#pragma unroll
+            for (int fj = 0; fj < 3; ++fj) y[r * 3 + fi] = fmaf(K[fi * 3 + fj], xv[fj], y[r * 3 + fi]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const size_t q = (size_t)(r * 3 + d) * np + n;
+          out[q] = fmaf(omega * kd[(size_t)n * 3 + d], bs[q] - y[r * 3 + d], in[q]);
+        }
+    }
+    __syncthreads();
+  }
+  for (size_t t = threadIdx.x; t < nv; t += blockDim.x) v.x[t] = xs[t];
+}
+
+// Bytes of shared memory k_mg_coarse_sweeps_smem needs on a level of np padded nodes.
+static size_t coarse_smem_bytes(size_t np, int nr) { return ((size_t)kEllPerNode + 9 * (size_t)nr + 3) * np * 4; }
+
 // The CG scalars after the level-0 post-smoother (last block of the instance, thread 0): setup sets rz, an
 // iteration beta and rz, for the right-hand sides still iterating.
 template <int NR>
@@ -796,15 +864,30 @@ int mgb_launch_mg_prolong(const MeshDev *mf, const MeshDev *mc, const Inst *inst
   return (int)cudaGetLastError();
 }
 
+int mgb_mg_init_attributes() {
+  int e = (int)cudaFuncSetAttribute(k_mg_coarse_sweeps_smem<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMgCoarseSmem);
+  if (e) return e;
+  return (int)cudaFuncSetAttribute(k_mg_coarse_sweeps_smem<6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kMgCoarseSmem);
+}
+
 int mgb_launch_mg_coarse_sweeps(const MeshDev *m, const Inst *insts, const int *list, int nlist, int nr, int l,
                                 int pairs, float omega, cudaStream_t s) {
   if (nlist <= 0 || pairs <= 0) return 0;
   if (l < 1 || m->nn > kMgCoarseNodes) return (int)cudaErrorInvalidValue;
   const dim3 g(1, nlist);
-  if (nr == 1)
+  const size_t smem = coarse_smem_bytes(m->np, nr);
+  if (smem <= (size_t)kMgCoarseSmem) {
+    if (nr == 1)
+      k_mg_coarse_sweeps_smem<1><<<g, kMgCoarseBlock, smem, s>>>(*m, insts, list, l, pairs, omega);
+    else
+      k_mg_coarse_sweeps_smem<6><<<g, kMgCoarseBlock, smem, s>>>(*m, insts, list, l, pairs, omega);
+  } else if (nr == 1) {
     k_mg_coarse_sweeps<1><<<g, kMgCoarseBlock, 0, s>>>(*m, insts, list, l, pairs, omega);
-  else
+  } else {
     k_mg_coarse_sweeps<6><<<g, kMgCoarseBlock, 0, s>>>(*m, insts, list, l, pairs, omega);
+  }
   return (int)cudaGetLastError();
 }
 
