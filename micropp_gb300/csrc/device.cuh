@@ -118,8 +118,8 @@ struct Inst {
   InstOut *out;
   // mixed form (FP32 Jacobian and CG vectors)
   float *vals32, *kinv32, *r32, *z32, *p32, *Ap32, *du32;
-  // Gauss-point tangent descriptors of the damage law for the symmetric FP32 Jacobian, written by the FP64
-  // residual: [(q * 8 + g) * nelem + e], q = 0: a, 1: c, 2..7: s  (C_gp = a C_el + c s s^T)
+  // Gauss-point tangent descriptors of the damage law for the symmetric FP32 Jacobian, written by the mixed
+  // form's residual kernel: [(q * 8 + g) * nelem + e], q = 0: a, 1: c, 2..7: s  (C_gp = a C_el + c s s^T)
   float *gpd;
   // implicit ctan: 6 right-hand sides; X6 (solutions) and F6 (right-hand sides) as double-float pairs hi + lo
   float *X6h, *X6l, *F6h, *F6l;

@@ -30,8 +30,9 @@ namespace {
 constexpr double kConstXg = 0.577350269189626;  // params.hpp:34
 constexpr double kDepsCtanAve = 1.0e-8;        // params.hpp:32
 
-// Tangent solve of the implicit ctan: FP32 CG sweeps to this relative tolerance, refined with FP64 residuals
-// until ||f_i - K x_i|| <= kTangentTol ||f_i|| for all six right-hand sides (at most kTangentSweeps sweeps).
+// Tangent solve of the implicit ctan: FP32 CG sweeps to this relative tolerance, refined with FP64-accurate
+// (double-float) residuals until ||f_i - K x_i|| <= kTangentTol ||f_i|| for all six right-hand sides (at most
+// kTangentSweeps sweeps).
 constexpr double kTangentSweepRel = 1.0e-5;
 constexpr double kTangentTol = 1.0e-9;
 // With a symmetric tangent (every phase elastic or damage) ctan takes the energy form from element energies,
@@ -1239,7 +1240,7 @@ std::vector<int> Engine::tangent_solve(const std::vector<int> &slots, bool use_m
 // graph: the FP32 assembly with the multigrid operators, the CG start (tolerances from d_eta_), a WHILE node
 // whose body runs a chunk of preconditioned CG iterations and then a kernel that continues the loop while some
 // listed instance still iterates (at most min(cg_max_its, kMgMaxIts) / kMgChunk + 2 chunks), u += du and the
-// FP64 residual.  The host's part of an iteration -- the tolerances before it, convergence, the line search and
+// residual.  The host's part of an iteration -- the tolerances before it, convergence, the line search and
 // the Jacobi redo of a capped solve after it -- stays outside.  A graph is built the first time a batch size
 // runs once the SpMV autotuner has picked that batch size's block (the autotuner times live launches, which a
 // capture cannot hold) and is replayed afterwards: its kernels read the listed instances and the tolerances
@@ -1417,7 +1418,7 @@ std::vector<NewtonResult> Engine::newton(const std::vector<int> &slots,
     }
     launches_ += 1;
     if (mixed) {
-      // Inexact Newton: the FP64 residual corrects each FP32 solve, so a correction only needs to gain the
+      // Inexact Newton: the FP64-accurate residual corrects each FP32 solve, so a correction only needs to gain the
       // digits still missing to the Newton tolerance: eta = 0.05 * nr_rel_tol * |b0| / |b_k|, kept within
       // [max(cg_rel_tol, kFp32CgFloor), 0.1] (an FP32 CG cannot reduce its residual much below 1e-6).
       std::vector<double> eta(active.size());

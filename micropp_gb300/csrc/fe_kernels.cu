@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(kMatElems * 24) k_elem_mat(MeshDev m, Mats mat
 //   damage  (C_g = a_g C + c_g s_g s_g^T):  Ke_ab = sum_g a_g K0_g,ab + c_g wg (B_a,g^T s_g)(B_b,g^T s_g)^T
 //   elastic:                               Ke_ab = sum_g K0_g,ab
 // with K0_g = wg B_g^T C_phase B_g precomputed per phase and Gauss point, and (a_g, c_g, s_g) written by the
-// FP64 residual at the same displacement.  The 8 warps of a block (one element position each) add their
+// residual kernel (k_elem_rhs_df) at the same displacement.  The 8 warps of a block (one element position each) add their
 // blocks into the block's 32 node rows (27 slots x 9) in shared memory in a fixed order; the rows are then
 // written once, coalesced.  No colouring, atomics or zeroing pass; boundary nodes get their real rows.
 constexpr int kAsmNodes = 32;

@@ -713,8 +713,8 @@ __global__ void k_t6_accumulate(MeshDev m, const Inst *insts, const int *list) {
 // phases, a symmetric tangent).  With v_i = w_i + x_i the tangent field of unit strain i (w_i the boundary lift,
 // x_i the interior solution X6h + X6l),
 //   ctan[k][i] = (1/V) sum_e sum_g wg eps(v_k)^T C_g eps(v_i),
-// C_g the Gauss-point tangent: the phase's elastic C, or for damage a C + c s s^T from the tangent terms the FP64
-// residual wrote.  The form is stationary at the exact x, so its error is quadratic in the error of x (the FP32
+// C_g the Gauss-point tangent: the phase's elastic C, or for damage a C + c s s^T from the tangent terms the
+// residual kernel wrote.  The form is stationary at the exact x, so its error is quadratic in the error of x (the FP32
 // solves and the FP32 rounding of the assembled tangent they used).  Summing element energies also avoids the
 // cancellation of v^T (K v) over assembled rows -- K v nearly vanishes on interior rows -- whose first-order
 // rounding with FP32 rows reached 1e-5 on 60^3 RVEs.  Block: kEnElems elements x 8 threads.  Thread a of an
