@@ -8,6 +8,7 @@
 
 #include "device.cuh"
 #include "df.cuh"
+#include "elem_df.cuh"
 #include "launch.h"
 #include "adjoint_laws.h"
 #include "hex_sumfact.h"
@@ -265,59 +266,28 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs_sf(MeshDev m, Mats mats
 }
 
 // ---------------------------------------------------------------------------------------------------
-// The element residual of k_elem_rhs_sf in double-float arithmetic (df.cuh), for elastic and damage phases.
-// The FP64 pipe issues 2 operations per SM and cycle, so the FP64 residual is bound by it; here the nodal
-// displacements are split into float pairs once, and the differences, the Gauss-point strains, the laws, the
-// stress sums and their transpose run on the FP32 pipe with about 46 bits (the residual's rounding stays near
-// 1e-13 of its terms).  Loads, the history, the element blocks and the average stress stay FP64.
-
-// Constants of an elastic or damage phase as double-float values.
-struct MatDf {
-  dfl lambda, two_mu, mu, xt_thr, r0, r1, q0, q1;
-};
-
-// The kernel's constants, split on the host: the phases, 1 - xg, 1 + xg, 1 / (4 h_d) and the Gauss weight.
-struct ResDf {
-  MatDf mat[3];
-  dfl cm, cp, inv4h[3], wg;
-};
-
-static dfl host_df(double v) {
-  const float h = (float)v;
-  return dfl{h, (float)(v - (double)h)};
-}
+// The element residual of k_elem_rhs_sf in double-float arithmetic, for elastic and damage phases: one thread
+// per element runs elem_rhs_df (elem_df.cuh).  The FP64 pipe issues 2 operations per SM and cycle, so the FP64
+// residual is bound by it; here the nodal displacements are split into float pairs once, and the differences,
+// the Gauss-point strains, the laws, the stress sums and their transpose run on the FP32 pipe with about 46
+// bits (the residual's rounding stays near 1e-13 of its terms).  Loads, the history, the element blocks and the
+// average stress stay FP64.
 
 static ResDf res_df(const MeshDev &m, const Mats &mats) {
   constexpr double kXg = 0.577350269189626;  // Gauss coordinate (params.hpp:34)
   ResDf c;
   for (int ph = 0; ph < 3; ++ph) {
     const MatDev &d = mats.m[ph];
-    c.mat[ph] = MatDf{host_df(d.lambda), host_df(d.two_mu), host_df(d.mu),     host_df(d.xt_thr),
-                      host_df(d.dmg_r0), host_df(d.dmg_r1), host_df(d.dmg_q0), host_df(d.dmg_q1)};
+    c.mat[ph] = MatDf{df_of(d.lambda), df_of(d.two_mu), df_of(d.mu),     df_of(d.xt_thr),
+                      df_of(d.dmg_r0), df_of(d.dmg_r1), df_of(d.dmg_q0), df_of(d.dmg_q1)};
   }
-  c.cm = host_df(1.0 - kXg);
-  c.cp = host_df(1.0 + kXg);
-  c.inv4h[0] = host_df(0.25 / m.dx);
-  c.inv4h[1] = host_df(0.25 / m.dy);
-  c.inv4h[2] = host_df(0.25 / m.dz);
-  c.wg = host_df(m.wg);
+  c.cm = df_of(1.0 - kXg);
+  c.cp = df_of(1.0 + kXg);
+  c.inv4h[0] = df_of(0.25 / m.dx);
+  c.inv4h[1] = df_of(0.25 / m.dy);
+  c.inv4h[2] = df_of(0.25 / m.dz);
+  c.wg = df_of(m.wg);
   return c;
-}
-
-// law_elastic (material.cpp:76-82)
-__device__ __forceinline__ void law_elastic_df(const MatDf &m, const dfl *eps, dfl *s) {
-  const dfl lt = m.lambda * (eps[0] + eps[1] + eps[2]);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) s[i] = lt + m.two_mu * eps[i];
-#pragma unroll
-  for (int i = 3; i < 6; ++i) s[i] = m.mu * eps[i];
-}
-
-// law_damage_hardening (material.cpp:213-225)
-__device__ __forceinline__ dfl hardening_df(const MatDf &m, dfl r) {
-  if (r < m.r0) return dfl{0.f, 0.f};
-  if (r < m.r1) return m.q0 + (r - m.r0) * 10.f;
-  return m.q1 + (r - m.r1) * 5.f;
 }
 
 __global__ void __launch_bounds__(kElemBlock) k_elem_rhs_df(MeshDev m, Mats mats, ResDf cst, const int8_t *etype,
@@ -330,147 +300,26 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_rhs_df(MeshDev m, Mats mats
   if (e < m.nelem) {
     const int ex = e % m.nex, ey = (e / m.nex) % m.ney, ez = e / (m.nex * m.ney);
     const int n0 = ez * m.nxny + ey * m.nx + ex;
-    // D[d][c][k]: the 36 nodal differences of hex_sumfact.h (sf::diffs)
-    dfl D[3][3][4];
-    {
-      dfl ue[24];
+    double ue[24];
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
+    for (int a = 0; a < 8; ++a) {
+      const int n = n0 + c_corner[a][2] * m.nxny + c_corner[a][1] * m.nx + c_corner[a][0];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) ue[a * 3 + d] = df_of(I.u[n * 3 + d]);
-      }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        int p, q;
-        sf::other_axes(d, p, q);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          int c1[3], c0[3];
-          c1[d] = 1;
-          c0[d] = 0;
-          c1[p] = c0[p] = k >> 1;
-          c1[q] = c0[q] = k & 1;
-          const int a1 = sf::node_of(c1[0], c1[1], c1[2]), a0 = sf::node_of(c0[0], c0[1], c0[2]);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) D[d][c][k] = ue[a1 * 3 + c] - ue[a0 * 3 + c];
-        }
-      }
+      for (int d = 0; d < 3; ++d) ue[a * 3 + d] = I.u[n * 3 + d];
     }
     const int ph = etype[e];
-    const MatDf &mf = cst.mat[ph];
-    const bool damage = mats.m[ph].type == 2;
-    const dfl cm = cst.cm, cp = cst.cp;  // 1 - xg, 1 + xg
-    const dfl *inv4h = cst.inv4h;
-    const dfl wg = cst.wg;
-    dfl S[3][3][4];
+    float *__restrict__ gpd = I.gpd;
+    const size_t st = (size_t)8 * m.nelem;
+    auto sink = [&](int g, float ta, float tc, const float *s6) {
+      const size_t o = (size_t)g * m.nelem + e;
+      gpd[o] = ta;
+      gpd[st + o] = tc;
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) S[d][c][k] = dfl{0.f, 0.f};
-#pragma unroll
-    for (int g = 0; g < 8; ++g) {
-      const int gs[3] = {(g == 1 || g == 2 || g == 5 || g == 6) ? 1 : -1, (g == 2 || g == 3 || g == 6 || g == 7) ? 1 : -1,
-                         g >= 4 ? 1 : -1};
-      // gradient at the point (sf::grad_at): (1 - x_p)(1 - x_q) ... weights of the four differences
-      dfl gr[3][3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        int p, q;
-        sf::other_axes(d, p, q);
-        const dfl mp = gs[p] > 0 ? cm : cp, pp = gs[p] > 0 ? cp : cm;  // 1 - x_p, 1 + x_p
-        const dfl mq = gs[q] > 0 ? cm : cp, pq = gs[q] > 0 ? cp : cm;  // 1 - x_q, 1 + x_q
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const dfl e0 = mq * D[d][c][0] + pq * D[d][c][1];
-          const dfl e1 = mq * D[d][c][2] + pq * D[d][c][3];
-          gr[d][c] = (mp * e0 + pp * e1) * inv4h[d];
-        }
-      }
-      const dfl eps[6] = {gr[0][0], gr[1][1], gr[2][2], gr[1][0] + gr[0][1], gr[2][0] + gr[0][2], gr[2][1] + gr[1][2]};
-      dfl sg[6];
-      law_elastic_df(mf, eps, sg);
-      if (damage) {
-        // law_damage_terms (laws.cuh) on the undamaged stress sg
-        const double *vg = I.vars_old ? I.vars_old + ((size_t)e * 8 + g) * kNvarGp : nullptr;
-        const dfl r_old = df_of(vg ? vg[0] : 0.0), D_old = df_of(vg ? vg[1] : 0.0);
-        dfl prod = sg[0] * eps[0];
-#pragma unroll
-        for (int i = 1; i < 6; ++i) prod = prod + sg[i] * eps[i];
-        const dfl r = df_nonneg(prod) ? df_sqrt(prod) : dfl{0.f, 0.f};
-        const dfl r_old_a = (r_old < mf.xt_thr) ? mf.xt_thr : r_old;
-        dfl Dm;
-        float ta, tc;
-        if (r <= r_old_a) {
-          Dm = D_old;
-          ta = (dfl{1.f, 0.f} - D_old).h;
-          tc = 0.f;
-        } else {
-          const dfl q = hardening_df(mf, r);
-          const dfl qr = q / r;
-          Dm = dfl{1.f, 0.f} - qr;
-          const float qp = (r < mf.r0) ? 0.f : (r < mf.r1 ? 10.f : 5.f);
-          ta = qr.h;
-          tc = (qp - ta) / (r.h * r.h);
-        }
-        float *__restrict__ gpd = I.gpd;
-        const size_t st = (size_t)8 * m.nelem, o = (size_t)g * m.nelem + e;
-        gpd[o] = ta;
-        gpd[st + o] = tc;
-#pragma unroll
-        for (int v = 0; v < 6; ++v) gpd[(2 + v) * st + o] = sg[v].h + sg[v].l;
-        const dfl f = dfl{1.f, 0.f} - Dm;
-#pragma unroll
-        for (int v = 0; v < 6; ++v) sg[v] = sg[v] * f;
-      }
-      // S[d][c][gp * 2 + gq] += wg sigma_dc (sf::accumulate), and the stress average
-      const dfl ws[6] = {sg[0] * wg, sg[1] * wg, sg[2] * wg, sg[3] * wg, sg[4] * wg, sg[5] * wg};
-      const dfl t[3][3] = {{ws[0], ws[3], ws[4]}, {ws[3], ws[1], ws[5]}, {ws[4], ws[5], ws[2]}};
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        int p, q;
-        sf::other_axes(d, p, q);
-        const int k = (gs[p] > 0 ? 2 : 0) + (gs[q] > 0 ? 1 : 0);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) S[d][c][k] = S[d][c][k] + t[d][c];
-      }
-#pragma unroll
-      for (int v = 0; v < 6; ++v) sav[v] = sav[v] + ws[v];
-    }
-    // be = the transpose (sf::finish)
+      for (int v = 0; v < 6; ++v) gpd[(2 + v) * st + o] = s6[v];
+    };
     dfl be[24];
-#pragma unroll
-    for (int i = 0; i < 24; ++i) be[i] = dfl{0.f, 0.f};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      int p, q;
-      sf::other_axes(d, p, q);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        dfl f[2][2];  // f[gp][cq]
-#pragma unroll
-        for (int gp = 0; gp < 2; ++gp) {
-          f[gp][0] = cp * S[d][c][gp * 2 + 0] + cm * S[d][c][gp * 2 + 1];
-          f[gp][1] = cm * S[d][c][gp * 2 + 0] + cp * S[d][c][gp * 2 + 1];
-        }
-#pragma unroll
-        for (int cpp = 0; cpp < 2; ++cpp)
-#pragma unroll
-          for (int cq = 0; cq < 2; ++cq) {
-            const dfl w = (cpp ? cm * f[0][cq] + cp * f[1][cq] : cp * f[0][cq] + cm * f[1][cq]) * inv4h[d];
-            int c1[3], c0[3];
-            c1[d] = 1;
-            c0[d] = 0;
-            c1[p] = c0[p] = cpp;
-            c1[q] = c0[q] = cq;
-            const int a1 = sf::node_of(c1[0], c1[1], c1[2]) * 3 + c, a0 = sf::node_of(c0[0], c0[1], c0[2]) * 3 + c;
-            be[a1] = be[a1] + w;
-            be[a0] = be[a0] - w;
-          }
-      }
-    }
+    elem_rhs_df(ue, cst.mat[ph], mats.m[ph].type == 2, cst,
+                I.vars_old ? I.vars_old + (size_t)e * 8 * kNvarGp : nullptr, kNvarGp, be, sav, sink);
     double *__restrict__ bev = I.be;
 #pragma unroll
     for (int i = 0; i < 24; ++i) bev[(size_t)i * m.nelem + e] = df_to_double(be[i]);
