@@ -1,8 +1,8 @@
 """Build recipe of the GB300 library: micropp_gb300/libmicropp_gb300.so (in-tree).
 
 CUDA sources are compiled by nvcc for sm_103a only; host C++ by g++; the whole library links the CUDA
-runtime statically, so it depends on nothing but the NVIDIA kernel driver (libcuda).  Translation units compile in parallel and a
-unit is rebuilt only when it or a header changed.  Run as ``python -m micropp_gb300.build`` or through
+runtime statically, so it depends on nothing but the NVIDIA kernel driver (libcuda).  Translation units
+compile in parallel and a unit is rebuilt only when it or a header changed.  Run as ``python -m micropp_gb300.build`` or through
 ``__graft_entry__.build()``.
 """
 import concurrent.futures as cf
